@@ -1,0 +1,349 @@
+"""K-SVD benchmark (one JSON line on stdout).
+
+Workload: the headline configuration n=256, K=1024, N=1,000,000, T=16 (seeded synthetic data of
+that shape and distribution: the reference's fMRI inputs are not published).  One "step" is one
+full K-SVD iteration (D'X, Batch-OMP, per-atom lists, the atom sweep, error/RMSE, Gram,
+clearDict) through ``ksvd_iterate`` with every input resident in HBM.  X is 1 GB, far larger
+than the 129 MB L2, so no L2 flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--precision fp32|mixed] [--config cfg2]
+
+--impl reference times the reference algorithm's CPU restatement (the oracle: the reference
+itself has no CPU path and cannot be built here) on the host cores, on a bounded sample of the
+same workload, scaled to the full workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+KERNELS_PER_CALL = 3          # pad copy, normcols, Gram before the first iteration
+KERNELS_PER_ITER = 14         # D'X, OMP, 6 list/precompute kernels, sweep, error, RMSE, Gram,
+#                               coherence, clearDict
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            m = json.load(f)
+        return dict(hbm=m["hbm_gbs"], bf16=m["bf16_tflops"], bf16_sus=m["bf16_tflops_sustained"],
+                    src="measured")
+    return dict(hbm=6800.0, bf16=1900.0, bf16_sus=1700.0, src="fallback")
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = max(mx, float(r[2]))
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def stage_bytes(cfg, N, stage):
+    """Algorithmic HBM bytes of one launch of each stage (FP32 data, 4-byte indices)."""
+    n, K, T = cfg.n, cfg.K, cfg.T
+    Kp = 128 if K <= 128 else 256 if K <= 256 else 512 if K <= 512 else 1024
+    if stage == "omp":      # stream alpha0 (Kp rows), write T (index, coefficient) + nnz
+        return N * (Kp * 4 + T * 8 + 4)
+    if stage == "sweep":    # gather x_s for every (signal, atom) entry, read the signal's code
+        #                     twice (a'D product and C refresh), write the new coefficient
+        return N * T * (n * 4) + 2 * N * T * T * 8 + N * T * 4
+    if stage == "lists":    # idx/nnz twice (count, fill), list write, X gathered per entry
+        return 2 * N * T * 4 + N * T * 4 + N * T * (n * 4 + T * 8)
+    if stage == "error":    # X once, the code once, the error vector
+        return N * n * 4 + N * T * 8 + N * 4
+    if stage == "dtx":      # X once, alpha0 written
+        return N * n * 4 + N * Kp * 4
+    return 0
+
+
+def stage_flops(cfg, N, stage):
+    n, K = cfg.n, cfg.K
+    if stage == "dtx":
+        return 2.0 * n * K * N
+    if stage == "gram":
+        return 2.0 * n * K * K
+    return 0.0
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def run_reference(args, cfg):
+    """The reference algorithm on the host cores (the oracle port), bounded sample."""
+    import numpy as np
+
+    import oracle
+    from ksvd_gb300 import datagen
+
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    oracle.build()
+    threads = oracle.num_threads()
+    Ns = min(cfg.N, args.cpu_sample)
+    p = datagen.make_problem(cfg, N=Ns)
+    X, D = p["X"], p["D"]
+    rng = np.random.default_rng(0)
+    times = []
+    for step in range(args.warmup + args.steps):
+        perm = rng.permutation(cfg.K).astype(np.int32)[None, :]
+        t0 = time.perf_counter()
+        D, idx, coef, nnz, rmse = oracle.ksvd(X, D, cfg.T, 1, perm)
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            times.append(dt)
+    t = statistics.median(times)
+    value = 1.0 / (t * cfg.N / Ns)          # iterations/s at the full N, linear in N
+    line = {
+        "impl": "reference", "metric": "ksvd_iters_per_s", "value": value, "unit": "iter/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded, %s shape)" % cfg.name,
+        "config": {"workload": "%s: n=%d K=%d N=%d T=%d, one K-SVD iteration per step"
+                   % (cfg.name, cfg.n, cfg.K, cfg.N, cfg.T), "n": cfg.n, "K": cfg.K,
+                   "N": cfg.N, "T": cfg.T},
+        "cpu_baseline": {"value": value, "unit": "iter/s", "cores": threads, "kind": "port",
+                         "sample": "%d of %d signals per step, median of %d steps, scaled by N"
+                         % (Ns, cfg.N, args.steps)},
+        "e2e": {"value": value, "unit": "iter/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def cpu_baseline(cfg, sample, reps=1):
+    import numpy as np
+
+    import oracle
+    from ksvd_gb300 import datagen
+
+    oracle.build()
+    Ns = min(cfg.N, sample)
+    p = datagen.make_problem(cfg, N=Ns)
+    perm = np.random.default_rng(0).permutation(cfg.K).astype(np.int32)[None, :]
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        oracle.ksvd(p["X"], p["D"], cfg.T, 1, perm)
+        ts.append(time.perf_counter() - t0)
+    t = statistics.median(ts)
+    return {"value": 1.0 / (t * cfg.N / Ns), "unit": "iter/s", "cores": oracle.num_threads(),
+            "kind": "port",
+            "sample": "one K-SVD iteration on %d of %d signals (%.2f s), scaled by N" %
+                      (Ns, cfg.N, t)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "mixed"])
+    ap.add_argument("--config", default="cfg2")
+    ap.add_argument("--cpu-sample", type=int, default=50000)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    from ksvd_gb300 import datagen
+
+    cfg = datagen.CONFIGS[args.config]
+    if args.impl == "reference":
+        return run_reference(args, cfg)
+
+    import numpy as np
+    import torch
+
+    ws, rank, local = dist_env()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from ksvd_gb300 import Handle
+
+    # CPU baseline first (before any CUDA work in this process), rank 0 at N=1 only
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        cpu = cpu_baseline(cfg, args.cpu_sample)
+
+    prob = datagen.make_problem(cfg, seed=datagen.SEED_BASE + cfg.index + 1000 * rank,
+                                device="cuda")
+    X, D = prob["X"], prob["D"]
+    N = X.shape[0]
+    h = Handle(cfg.n, cfg.K, cfg.T, precision=args.precision, profile=True)
+    idx, coef, nnz = h._code(N, dev)
+    out = (idx, coef, nnz)
+    rms = []
+    for _ in range(args.warmup):
+        rms += list(h.iterate(D, X, 1, out=out)[3])
+    h.stage_times(reset=True)
+    sampler = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t_wall = time.perf_counter()
+    e0.record(stream)
+    for _ in range(args.steps):
+        rms += list(h.iterate(D, X, 1, out=out)[3])
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    st = h.stage_times()
+    value = ws * args.steps / (ms / 1e3)
+
+    # dominant stage and its roofline
+    pk = peaks()
+    per = {k: (v[0] / max(v[1], 1), v[1]) for k, v in st.items() if v[1] > 0}
+    dom = max(per, key=lambda k: per[k][0] * per[k][1])
+    launch_ms = per[dom][0]
+    if dom in ("dtx", "gram") and args.precision == "mixed":
+        ach = stage_flops(cfg, N, dom) / (launch_ms / 1e3) / 1e12
+        roof = {"bound": "tensor", "achieved": ach, "peak": pk["bf16"], "unit": "TFLOP/s",
+                "frac": ach / pk["bf16"], "traffic": None}
+    else:
+        ach = stage_bytes(cfg, N, dom) / (launch_ms / 1e3) / 1e9
+        roof = {"bound": "hbm", "achieved": ach, "peak": pk["hbm"], "unit": "GB/s",
+                "frac": ach / pk["hbm"], "traffic": None}
+    roof["kernel"] = dom
+    roof["peak_source"] = pk["src"]
+    stage_summary = {k: {"ms_per_launch": round(v[0], 4), "share": round(v[0] * v[1] / sum(
+        a * b for a, b in per.values()), 4)} for k, v in per.items()}
+    omp_ms = per.get("omp", (0, 0))[0] + per.get("dtx", (0, 0))[0]
+
+    # end to end through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        Xh = torch.empty((N, cfg.n), dtype=torch.float32, pin_memory=True)
+        Xh.copy_(X)
+        Dh = torch.empty((cfg.K, cfg.n), dtype=torch.float32, pin_memory=True)
+        Dh.copy_(D)
+        Xn = Xh.numpy().T          # (n, N) column-major view of the pinned buffer
+        Dn = Dh.numpy().T
+        oi = torch.empty((N, cfg.T), dtype=torch.int32, pin_memory=True).numpy()
+        oc = torch.empty((N, cfg.T), dtype=torch.float32, pin_memory=True).numpy()
+        on = torch.empty((N,), dtype=torch.int32, pin_memory=True).numpy()
+        h.iterate_host(Dn, Xn, 1, out=(oi, oc, on))          # warm the staging buffers
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_steps = max(1, min(args.steps, 5))
+        for _ in range(e2e_steps):
+            h.iterate_host(Dn, Xn, 1, out=(oi, oc, on))
+        torch.cuda.synchronize()
+        te = time.perf_counter() - t0
+        if dist:
+            t = torch.tensor([te], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            te = float(t.item())
+        e2e = {"value": ws * e2e_steps / te, "unit": "iter/s",
+               "h2d_bytes_per_step": int(X.numel() * 4 + D.numel() * 4),
+               "d2h_bytes_per_step": int(D.numel() * 4 + N * cfg.T * 8 + N * 4 + 8),
+               "steps": e2e_steps}
+    if rank == 0:
+        line = {
+            "metric": "ksvd_iters_per_s", "value": value, "unit": "iter/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32" if args.precision == "fp32" else "bf16-mixed",
+            "data": "synthetic (seeded, %s shape; reference data unpublished)" % cfg.name,
+            "config": {"workload": "%s: n=%d K=%d N=%d T=%d, one K-SVD iteration per step"
+                       % (cfg.name, cfg.n, cfg.K, N, cfg.T), "n": cfg.n, "K": cfg.K, "N": N,
+                       "T": cfg.T, "precision": args.precision,
+                       "parallelism": "replicas%d" % ws if ws > 1 else "single",
+                       "l2": "inputs larger than L2 (X = %.2f GB)" % (X.numel() * 4 / 1e9)},
+            "omp_signals_per_s": {"value": ws * N / (omp_ms / 1e3) if omp_ms else None,
+                                  "unit": "signals/s", "stages": "D'X + Batch-OMP"},
+            "stages": stage_summary,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": args.steps * (KERNELS_PER_CALL + KERNELS_PER_ITER),
+            "clocks": clocks,
+            "rmse_last": rms[-1] if rms else None,
+            "wall_s_timed": t_wall,
+        }
+        print(json.dumps(line), flush=True)
+    h.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,648 @@
+// api.cu -- the C ABI (include/ksvd_gb300.h): handle, device workspace and the host-side
+// orchestration of the K-SVD iteration.  Replaces the reference's KSVD / OMP /
+// DictionaryUpdate classes (KSVD.cu, OMP.cu, DictionaryUpdate.cu), its enum-indexed
+// DeviceMemory pool (DeviceMemory.cu:19-138) and its cuBLAS handle base (CudaAlgorithm.cu).
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/ksvd_gb300.h"
+#include "common.cuh"
+#include "kernels.cuh"
+
+using namespace ksvd;
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+};
+
+}  // namespace
+
+struct ksvd_handle {
+  ksvd_params p{};
+  int Kp = 0;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  std::string err;
+  std::vector<DevBuf> bufs;
+  // stage state (what the last update / error call left behind)
+  int64_t update_N = -1;
+  int64_t error_N = -1;
+  int64_t perm_draws = 0;
+  // stage profiling (KSVD_FLAG_PROFILE)
+  struct Pending { int stage; cudaEvent_t a, b; };
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  std::vector<Pending> pending;
+  double stage_ms[8] = {0};
+  int64_t stage_calls[8] = {0};
+  bool profiling() const { return (p.flags & KSVD_FLAG_PROFILE) != 0; }
+};
+
+namespace {
+
+enum BufId {
+  B_DPAD, B_G, B_A0, B_XN2, B_LIST, B_START, B_BHIST, B_Y, B_GN2, B_C, B_AVEC, B_AD, B_PART,
+  B_UNUSED, B_BITMAP, B_REPLACED, B_COUNTER, B_USE, B_BARRIER, B_ERR, B_PSUM, B_BVAL, B_BIDX,
+  B_RMSE, B_M, B_MI, B_CLEARED, B_DEVERR, B_PERM, B_GPAD_IN, B_HX, B_HD, B_HIDX, B_HCOEF, B_HNNZ,
+  B_COUNT
+};
+
+ksvd_status fail(ksvd_handle* h, ksvd_status s, const char* fmt, const char* detail = nullptr) {
+  if (h) {
+    char buf[512];
+    std::snprintf(buf, sizeof(buf), fmt, detail ? detail : "");
+    h->err = buf;
+  }
+  return s;
+}
+
+ksvd_status cuda_fail(ksvd_handle* h, cudaError_t e, const char* where) {
+  if (h) h->err = std::string(where) + ": " + cudaGetErrorString(e);
+  cudaGetLastError();
+  if (e == cudaErrorMemoryAllocation) return KSVD_ERR_OUT_OF_MEMORY;
+  return KSVD_ERR_CUDA;
+}
+
+#define KSVD_CK(h, call)                                   \
+  do {                                                     \
+    cudaError_t e_ = (call);                               \
+    if (e_ != cudaSuccess) return cuda_fail(h, e_, #call); \
+  } while (0)
+
+#define KSVD_TRY(expr)                     \
+  do {                                     \
+    ksvd_status s_ = (expr);               \
+    if (s_ != KSVD_OK) return s_;          \
+  } while (0)
+
+template <typename T>
+ksvd_status ensure(ksvd_handle* h, BufId id, size_t count, T** out) {
+  DevBuf& b = h->bufs[id];
+  const size_t bytes = count * sizeof(T) + 256;
+  if (b.cap < bytes) {
+    if (b.p) {
+      cudaStreamSynchronize(h->stream);
+      cudaFree(b.p);
+      b.p = nullptr;
+      b.cap = 0;
+    }
+    cudaError_t e = cudaMalloc(&b.p, bytes);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc(workspace)");
+    b.cap = bytes;
+  }
+  *out = reinterpret_cast<T*>(b.p);
+  return KSVD_OK;
+}
+
+ksvd_status check_params(const ksvd_params* p, ksvd_handle* h) {
+  if (!p) return fail(h, KSVD_ERR_INVALID_ARGUMENT, "null params%s");
+  if (p->n < 1 || p->K < 1 || p->T < 1) return fail(h, KSVD_ERR_INVALID_ARGUMENT, "n, K, T must be >= 1%s");
+  if (p->K > kMaxK) return fail(h, KSVD_ERR_UNSUPPORTED, "K > 1024 is not supported%s");
+  if (p->T > kMaxT) return fail(h, KSVD_ERR_UNSUPPORTED, "T > 64 is not supported%s");
+  if (p->n > kMaxN) return fail(h, KSVD_ERR_UNSUPPORTED, "n > 1024 is not supported%s");
+  if (p->T > p->K) return fail(h, KSVD_ERR_INVALID_ARGUMENT, "T must be <= K%s");
+  if (p->precision != KSVD_PREC_FP32 && p->precision != KSVD_PREC_MIXED)
+    return fail(h, KSVD_ERR_INVALID_ARGUMENT, "unknown precision%s");
+  if (p->max_replace_signals < 1) return fail(h, KSVD_ERR_INVALID_ARGUMENT, "max_replace_signals must be >= 1%s");
+  return KSVD_OK;
+}
+
+ksvd_status check_dev_err(ksvd_handle* h) {
+  int* de = nullptr;
+  KSVD_TRY(ensure(h, B_DEVERR, 1, &de));
+  int v = 0;
+  KSVD_CK(h, cudaMemcpyAsync(&v, de, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  KSVD_CK(h, cudaStreamSynchronize(h->stream));
+  if (v == 0) return KSVD_OK;
+  KSVD_CK(h, cudaMemsetAsync(de, 0, sizeof(int), h->stream));
+  if (v & kDevErrTimeout) return fail(h, KSVD_ERR_TIMEOUT, "a device-side grid barrier timed out%s");
+  if (v & kDevErrBounds) return fail(h, KSVD_ERR_INVALID_ARGUMENT, "sparse code holds an atom index outside [0, K)%s");
+  return fail(h, KSVD_ERR_NUMERIC, "NaN or Inf met on the device%s");
+}
+
+uint64_t splitmix64(uint64_t& x) {
+  uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+cudaEvent_t next_event(ksvd_handle* h) {
+  if (h->ev_used == h->ev_pool.size()) {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    h->ev_pool.push_back(e);
+  }
+  return h->ev_pool[h->ev_used++];
+}
+
+// Brackets one stage with events on the handle's stream when profiling is on.
+struct StageScope {
+  ksvd_handle* h;
+  int stage;
+  cudaEvent_t a = nullptr;
+  StageScope(ksvd_handle* hh, int s) : h(hh), stage(s) {
+    if (h->profiling() && (a = next_event(h))) cudaEventRecord(a, h->stream);
+  }
+  ~StageScope() {
+    if (!a) return;
+    cudaEvent_t b = next_event(h);
+    if (!b) return;
+    cudaEventRecord(b, h->stream);
+    h->pending.push_back({stage, a, b});
+  }
+};
+
+void collect_stage_times(ksvd_handle* h) {
+  for (const auto& p : h->pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      h->stage_ms[p.stage] += ms;
+      h->stage_calls[p.stage] += 1;
+    }
+  }
+  h->pending.clear();
+  h->ev_used = 0;
+  cudaGetLastError();
+}
+
+// Working copy of a user dictionary (n x K) in the zero-padded n x Kp buffer.
+ksvd_status load_dict(ksvd_handle* h, const float* D, float** Dp) {
+  const int n = h->p.n, K = h->p.K, Kp = h->Kp;
+  KSVD_TRY(ensure(h, B_DPAD, (size_t)n * Kp, Dp));
+  KSVD_CK(h, launch_copy_pad_cols(D, n, K, *Dp, Kp, h->stream));
+  return KSVD_OK;
+}
+
+ksvd_status store_dict(ksvd_handle* h, const float* Dp, float* D) {
+  const size_t bytes = sizeof(float) * (size_t)h->p.n * h->p.K;
+  KSVD_CK(h, cudaMemcpyAsync(D, Dp, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  return KSVD_OK;
+}
+
+// G = D'D for the padded working dictionary (Kp x Kp, zero padded)
+ksvd_status gram_padded(ksvd_handle* h, const float* Dp, float* G) {
+  StageScope sc(h, KSVD_STAGE_GRAM);
+  const int n = h->p.n, K = h->p.K, Kp = h->Kp;
+  KSVD_CK(h, launch_gemm_tn_f32(Dp, n, Dp, n, G, Kp, K, Kp, K, Kp, n, h->stream));
+  return KSVD_OK;
+}
+
+// alpha0 = D'X into the Kp x N buffer (rows K..Kp-1 zero)
+ksvd_status dtx_padded(ksvd_handle* h, const float* Dp, const float* X, int64_t N, float* A0) {
+  StageScope sc(h, KSVD_STAGE_DTX);
+  const int n = h->p.n, K = h->p.K, Kp = h->Kp;
+  KSVD_CK(h, launch_gemm_tn_f32(Dp, n, X, n, A0, Kp, K, Kp, N, N, n, h->stream));
+  return KSVD_OK;
+}
+
+ksvd_status run_omp(ksvd_handle* h, const float* G, const float* A0, int64_t N,
+                    const float* xnorm2, const float* eps2, int32_t* idx, float* coef,
+                    int32_t* nnz) {
+  int* de = nullptr;
+  KSVD_TRY(ensure(h, B_DEVERR, 1, &de));
+  StageScope sc(h, KSVD_STAGE_OMP);
+  KSVD_CK(h, launch_omp(G, h->Kp, A0, h->Kp, h->p.K, N, h->p.T, xnorm2, eps2, idx, coef, nnz, de,
+                        h->stream));
+  return KSVD_OK;
+}
+
+struct UpdateWs {
+  UpdateArgs u;
+};
+
+ksvd_status update_ws(ksvd_handle* h, int64_t N, UpdateArgs& u) {
+  const int n = h->p.n, Kp = h->Kp;
+  const int64_t nblk = update_block_count(N);
+  const int nctas = update_sweep_ctas();
+  std::memset(&u, 0, sizeof(u));
+  KSVD_TRY(ensure(h, B_LIST, (size_t)N * h->p.T, &u.list));
+  KSVD_TRY(ensure(h, B_START, (size_t)Kp + 1, &u.start));
+  KSVD_TRY(ensure(h, B_BHIST, (size_t)Kp * nblk, &u.block_hist));
+  KSVD_TRY(ensure(h, B_Y, (size_t)n * Kp, &u.Y));
+  KSVD_TRY(ensure(h, B_GN2, (size_t)Kp, &u.gn2));
+  KSVD_TRY(ensure(h, B_C, (size_t)Kp * Kp, &u.C));
+  KSVD_TRY(ensure(h, B_AVEC, (size_t)2 * n, &u.avec));
+  KSVD_TRY(ensure(h, B_AD, (size_t)Kp, &u.aD));
+  KSVD_TRY(ensure(h, B_PART, (size_t)4 * (nctas + 1), &u.part));
+  KSVD_TRY(ensure(h, B_UNUSED, (size_t)N, &u.unused));
+  KSVD_TRY(ensure(h, B_BITMAP, (size_t)N, &u.bitmap));
+  KSVD_TRY(ensure(h, B_REPLACED, (size_t)Kp, &u.replaced));
+  KSVD_TRY(ensure(h, B_COUNTER, 1, &u.counter));
+  KSVD_TRY(ensure(h, B_USE, (size_t)Kp, &u.usecount));
+  KSVD_TRY(ensure(h, B_BARRIER, 2, &u.barrier));
+  KSVD_TRY(ensure(h, B_DEVERR, 1, &u.dev_err));
+  u.n = n; u.K = h->p.K; u.Kp = Kp; u.T = h->p.T; u.N = N;
+  u.max_signals = h->p.max_replace_signals;
+  return KSVD_OK;
+}
+
+ksvd_status run_update(ksvd_handle* h, float* Dp, const float* X, int64_t N, const int32_t* idx,
+                       float* coef, const int32_t* nnz, const int32_t* perm_dev) {
+  UpdateArgs u;
+  KSVD_TRY(update_ws(h, N, u));
+  u.X = X; u.D = Dp; u.idx = idx; u.coef = coef; u.nnz = nnz; u.perm = perm_dev;
+  {
+    StageScope sc(h, KSVD_STAGE_LISTS);
+    KSVD_CK(h, launch_update_prepare(u, h->stream));
+  }
+  {
+    StageScope sc(h, KSVD_STAGE_SWEEP);
+    KSVD_CK(h, launch_update_sweep(u, h->stream));
+  }
+  h->update_N = N;
+  return KSVD_OK;
+}
+
+ksvd_status run_error(ksvd_handle* h, const float* Dp, const float* X, int64_t N,
+                      const int32_t* idx, const float* coef, const int32_t* nnz,
+                      double* rmse_dev_slot) {
+  ErrorArgs a;
+  std::memset(&a, 0, sizeof(a));
+  const int64_t nb = error_block_count(N);
+  KSVD_TRY(ensure(h, B_ERR, (size_t)N, &a.err));
+  KSVD_TRY(ensure(h, B_PSUM, (size_t)nb, &a.part_sum));
+  KSVD_TRY(ensure(h, B_BVAL, (size_t)nb, &a.bucket_val));
+  KSVD_TRY(ensure(h, B_BIDX, (size_t)nb, &a.bucket_idx));
+  a.n = h->p.n; a.K = h->p.K; a.Kp = h->Kp; a.T = h->p.T; a.N = N;
+  a.X = X; a.D = Dp; a.idx = idx; a.coef = coef; a.nnz = nnz;
+  int32_t* bm = nullptr;
+  if (h->update_N == N) KSVD_TRY(ensure(h, B_BITMAP, (size_t)N, &bm));
+  a.bitmap = bm;
+  a.rmse_out = rmse_dev_slot;
+  StageScope sc(h, KSVD_STAGE_ERROR);
+  KSVD_CK(h, launch_error(a, h->stream));
+  h->error_N = N;
+  return KSVD_OK;
+}
+
+ksvd_status run_clear(ksvd_handle* h, float* Dp, float* G, const float* X, int64_t N,
+                      int32_t* cleared_dev) {
+  ClearArgs c;
+  std::memset(&c, 0, sizeof(c));
+  const int Kp = h->Kp;
+  c.n = h->p.n; c.K = h->p.K; c.Kp = Kp; c.N = N; c.X = X; c.D = Dp; c.G = G;
+  int32_t *use = nullptr, *rep = nullptr;
+  KSVD_TRY(ensure(h, B_USE, (size_t)Kp, &use));
+  KSVD_TRY(ensure(h, B_REPLACED, (size_t)Kp, &rep));
+  c.usecount = use; c.replaced = rep;
+  const int64_t nb = error_block_count(N);
+  KSVD_TRY(ensure(h, B_ERR, (size_t)N, &c.err));
+  KSVD_TRY(ensure(h, B_BVAL, (size_t)nb, &c.bucket_val));
+  KSVD_TRY(ensure(h, B_BIDX, (size_t)nb, &c.bucket_idx));
+  c.nbuckets = nb;
+  c.mu_thresh = h->p.mu_thresh;
+  c.use_thresh = h->p.use_thresh;
+  c.cleared = cleared_dev;
+  float* m = nullptr;
+  int* mi = nullptr;
+  KSVD_TRY(ensure(h, B_M, (size_t)Kp, &m));
+  KSVD_TRY(ensure(h, B_MI, (size_t)Kp, &mi));
+  StageScope sc(h, KSVD_STAGE_CLEAR);
+  KSVD_CK(h, launch_clear_dict(c, m, mi, h->stream));
+  return KSVD_OK;
+}
+
+ksvd_status upload_perm(ksvd_handle* h, const int32_t* perms_host, int32_t iters, int32_t** out) {
+  const int K = h->p.K;
+  std::vector<int32_t> tmp;
+  if (!perms_host) {
+    tmp.resize((size_t)iters * K);
+    for (int32_t it = 0; it < iters; ++it)
+      ksvd_random_permutation(h->p.seed, h->perm_draws + it, K, tmp.data() + (size_t)it * K);
+    h->perm_draws += iters;
+    perms_host = tmp.data();
+  } else {
+    std::vector<char> seen(K);
+    for (int32_t it = 0; it < iters; ++it) {
+      std::fill(seen.begin(), seen.end(), 0);
+      for (int k = 0; k < K; ++k) {
+        const int32_t v = perms_host[(size_t)it * K + k];
+        if (v < 0 || v >= K || seen[v])
+          return fail(h, KSVD_ERR_INVALID_ARGUMENT, "perms must hold permutations of 0..K-1%s");
+        seen[v] = 1;
+      }
+    }
+  }
+  int32_t* d = nullptr;
+  KSVD_TRY(ensure(h, B_PERM, (size_t)iters * K, &d));
+  KSVD_CK(h, cudaMemcpyAsync(d, perms_host, sizeof(int32_t) * (size_t)iters * K,
+                             cudaMemcpyHostToDevice, h->stream));
+  KSVD_CK(h, cudaStreamSynchronize(h->stream));   // perms_host may be a temporary
+  *out = d;
+  return KSVD_OK;
+}
+
+bool bad_ptr(const void* p) { return p == nullptr; }
+
+
+}  // namespace
+
+// ============================================================================================
+extern "C" {
+
+void ksvd_default_params(ksvd_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->T = 6;                        // ProgramParameters.cuh:20
+  p->precision = KSVD_PREC_FP32;
+  p->mu_thresh = 0.8f;             // ProgramParameters.cuh:23
+  p->use_thresh = 4;               // GlobalDeclarations.cuh:54
+  p->max_replace_signals = 5000;   // GlobalDeclarations.cuh:63
+  p->seed = 0x4B535644ull;
+}
+
+int32_t ksvd_abi_version(void) { return KSVD_GB300_ABI_VERSION; }
+
+const char* ksvd_status_string(ksvd_status s) {
+  switch (s) {
+    case KSVD_OK: return "ok";
+    case KSVD_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case KSVD_ERR_UNSUPPORTED: return "unsupported size";
+    case KSVD_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case KSVD_ERR_CUDA: return "CUDA error";
+    case KSVD_ERR_NUMERIC: return "NaN or Inf encountered";
+    case KSVD_ERR_TIMEOUT: return "device-side wait timed out";
+    case KSVD_ERR_STATE: return "stage called out of order";
+  }
+  return "unknown status";
+}
+
+const char* ksvd_last_error(const ksvd_handle* h) { return h ? h->err.c_str() : ""; }
+
+int64_t ksvd_workspace_bytes(const ksvd_handle* h) {
+  if (!h) return 0;
+  int64_t t = 0;
+  for (const auto& b : h->bufs) t += (int64_t)b.cap;
+  return t;
+}
+
+ksvd_status ksvd_random_permutation(uint64_t seed, int64_t iteration, int32_t K, int32_t* perm) {
+  if (!perm || K < 1) return KSVD_ERR_INVALID_ARGUMENT;
+  uint64_t st = seed ^ (0xD1B54A32D192ED03ull * (uint64_t)(iteration + 1));
+  for (int32_t k = 0; k < K; ++k) perm[k] = k;
+  for (int32_t k = K - 1; k > 0; --k) {       // Fisher-Yates
+    const uint64_t r = splitmix64(st) % (uint64_t)(k + 1);
+    const int32_t t = perm[k];
+    perm[k] = perm[r];
+    perm[r] = t;
+  }
+  return KSVD_OK;
+}
+
+ksvd_status ksvd_create(ksvd_handle** out, const ksvd_params* params, void* stream) {
+  if (!out) return KSVD_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  ksvd_status s = check_params(params, nullptr);
+  if (s != KSVD_OK) return s;
+  ksvd_handle* h = new (std::nothrow) ksvd_handle();
+  if (!h) return KSVD_ERR_OUT_OF_MEMORY;
+  h->p = *params;
+  h->Kp = omp_padded_k(params->K);
+  h->stream = reinterpret_cast<cudaStream_t>(stream);
+  h->bufs.resize(B_COUNT);
+  cudaError_t e = cudaGetDevice(&h->device);
+  if (e != cudaSuccess) {
+    delete h;
+    cudaGetLastError();
+    return KSVD_ERR_CUDA;
+  }
+  int* de = nullptr;
+  if ((s = ensure(h, B_DEVERR, 1, &de)) != KSVD_OK) { delete h; return s; }
+  if (cudaMemsetAsync(de, 0, sizeof(int), h->stream) != cudaSuccess) {
+    ksvd_destroy(h);
+    cudaGetLastError();
+    return KSVD_ERR_CUDA;
+  }
+  *out = h;
+  return KSVD_OK;
+}
+
+void ksvd_destroy(ksvd_handle* h) {
+  if (!h) return;
+  cudaStreamSynchronize(h->stream);
+  for (auto& b : h->bufs)
+    if (b.p) cudaFree(b.p);
+  for (auto e : h->ev_pool) cudaEventDestroy(e);
+  delete h;
+}
+
+ksvd_status ksvd_read_stage_times(ksvd_handle* h, ksvd_stage_times* out, int32_t reset) {
+  if (!h || !out) return KSVD_ERR_INVALID_ARGUMENT;
+  KSVD_CK(h, cudaStreamSynchronize(h->stream));
+  collect_stage_times(h);
+  for (int i = 0; i < 8; ++i) {
+    out->ms[i] = h->stage_ms[i];
+    out->calls[i] = h->stage_calls[i];
+    if (reset) { h->stage_ms[i] = 0; h->stage_calls[i] = 0; }
+  }
+  return KSVD_OK;
+}
+
+ksvd_status ksvd_synchronize(ksvd_handle* h) {
+  if (!h) return KSVD_ERR_INVALID_ARGUMENT;
+  KSVD_CK(h, cudaStreamSynchronize(h->stream));
+  collect_stage_times(h);
+  KSVD_CK(h, cudaGetLastError());
+  return check_dev_err(h);
+}
+
+ksvd_status ksvd_normcols(ksvd_handle* h, float* D) {
+  if (!h || bad_ptr(D)) return KSVD_ERR_INVALID_ARGUMENT;
+  KSVD_CK(h, launch_normcols(D, h->p.n, h->p.K, h->stream));
+  return KSVD_OK;
+}
+
+ksvd_status ksvd_gram(ksvd_handle* h, const float* D, float* G) {
+  if (!h || bad_ptr(D) || bad_ptr(G)) return KSVD_ERR_INVALID_ARGUMENT;
+  const int n = h->p.n, K = h->p.K;
+  KSVD_CK(h, launch_gemm_tn_f32(D, n, D, n, G, K, K, K, K, K, n, h->stream));
+  return KSVD_OK;
+}
+
+ksvd_status ksvd_dtx(ksvd_handle* h, const float* D, const float* X, int64_t N, float* A0) {
+  if (!h || bad_ptr(D) || bad_ptr(X) || bad_ptr(A0) || N < 0) return KSVD_ERR_INVALID_ARGUMENT;
+  const int n = h->p.n, K = h->p.K;
+  KSVD_CK(h, launch_gemm_tn_f32(D, n, X, n, A0, K, K, K, N, N, n, h->stream));
+  return KSVD_OK;
+}
+
+ksvd_status ksvd_omp_gram(ksvd_handle* h, const float* G, const float* A0, int64_t N,
+                          const float* xnorm2, const float* eps2, int32_t* idx, float* coef,
+                          int32_t* nnz) {
+  if (!h || bad_ptr(G) || bad_ptr(A0) || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || N < 0)
+    return KSVD_ERR_INVALID_ARGUMENT;
+  if (eps2 && !xnorm2) return fail(h, KSVD_ERR_INVALID_ARGUMENT, "eps2 needs xnorm2%s");
+  if (N == 0) return KSVD_OK;
+  const int K = h->p.K, Kp = h->Kp;
+  float *Gp = nullptr, *Ap = nullptr;
+  KSVD_TRY(ensure(h, B_GPAD_IN, (size_t)Kp * Kp, &Gp));
+  KSVD_TRY(ensure(h, B_A0, (size_t)Kp * N, &Ap));
+  KSVD_CK(h, cudaMemsetAsync(Gp, 0, sizeof(float) * (size_t)Kp * Kp, h->stream));
+  KSVD_CK(h, launch_copy_matrix(G, K, Gp, Kp, K, K, h->stream));
+  if (Kp != K) KSVD_CK(h, cudaMemsetAsync(Ap, 0, sizeof(float) * (size_t)Kp * N, h->stream));
+  KSVD_CK(h, launch_copy_matrix(A0, K, Ap, Kp, K, N, h->stream));
+  return run_omp(h, Gp, Ap, N, xnorm2, eps2, idx, coef, nnz);
+}
+
+ksvd_status ksvd_omp(ksvd_handle* h, const float* D, const float* X, int64_t N, const float* eps2,
+                     int32_t* idx, float* coef, int32_t* nnz) {
+  if (!h || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || N < 0)
+    return KSVD_ERR_INVALID_ARGUMENT;
+  if (N == 0) return KSVD_OK;
+  float *Dp = nullptr, *G = nullptr, *A0 = nullptr, *xn2 = nullptr;
+  KSVD_TRY(load_dict(h, D, &Dp));
+  KSVD_TRY(ensure(h, B_G, (size_t)h->Kp * h->Kp, &G));
+  KSVD_TRY(ensure(h, B_A0, (size_t)h->Kp * N, &A0));
+  KSVD_TRY(gram_padded(h, Dp, G));
+  KSVD_TRY(dtx_padded(h, Dp, X, N, A0));
+  if (eps2) {
+    KSVD_TRY(ensure(h, B_XN2, (size_t)N, &xn2));
+    KSVD_CK(h, launch_col_norm2(X, h->p.n, N, xn2, h->stream));
+  }
+  return run_omp(h, G, A0, N, xn2, eps2, idx, coef, nnz);
+}
+
+ksvd_status ksvd_update_dictionary(ksvd_handle* h, float* D, const float* X, int64_t N,
+                                   const int32_t* idx, float* coef, const int32_t* nnz,
+                                   const int32_t* perm) {
+  if (!h || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || N < 1)
+    return KSVD_ERR_INVALID_ARGUMENT;
+  if ((int64_t)N * h->p.T > 0x7fffffffLL)
+    return fail(h, KSVD_ERR_UNSUPPORTED, "N*T must stay below 2^31%s");
+  float* Dp = nullptr;
+  KSVD_TRY(load_dict(h, D, &Dp));
+  const int32_t* pd = perm;
+  if (!pd) {
+    int32_t* tmp = nullptr;
+    KSVD_TRY(upload_perm(h, nullptr, 1, &tmp));
+    pd = tmp;
+  }
+  KSVD_TRY(run_update(h, Dp, X, N, idx, coef, nnz, pd));
+  KSVD_TRY(store_dict(h, Dp, D));
+  return KSVD_OK;
+}
+
+ksvd_status ksvd_error(ksvd_handle* h, const float* D, const float* X, int64_t N,
+                       const int32_t* idx, const float* coef, const int32_t* nnz, float* err,
+                       double* rmse) {
+  if (!h || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || N < 1)
+    return KSVD_ERR_INVALID_ARGUMENT;
+  float* Dp = nullptr;
+  double* rd = nullptr;
+  KSVD_TRY(load_dict(h, D, &Dp));
+  KSVD_TRY(ensure(h, B_RMSE, 1024, &rd));
+  KSVD_TRY(run_error(h, Dp, X, N, idx, coef, nnz, rd));
+  if (err) {
+    float* e = nullptr;
+    KSVD_TRY(ensure(h, B_ERR, (size_t)N, &e));
+    KSVD_CK(h, cudaMemcpyAsync(err, e, sizeof(float) * N, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  if (rmse) {
+    KSVD_CK(h, cudaMemcpyAsync(rmse, rd, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    KSVD_CK(h, cudaStreamSynchronize(h->stream));
+    return check_dev_err(h);
+  }
+  return KSVD_OK;
+}
+
+ksvd_status ksvd_clear_dict(ksvd_handle* h, float* D, const float* X, int64_t N,
+                            const int32_t* idx, const float* coef, const int32_t* nnz,
+                            int32_t* cleared) {
+  if (!h || bad_ptr(D) || bad_ptr(X) || N < 1) return KSVD_ERR_INVALID_ARGUMENT;
+  (void)idx; (void)coef; (void)nnz;
+  if (h->update_N != N || h->error_N != N)
+    return fail(h, KSVD_ERR_STATE,
+                "clear_dict needs ksvd_update_dictionary and ksvd_error on the same N first%s");
+  float *Dp = nullptr, *G = nullptr;
+  int32_t* cd = nullptr;
+  KSVD_TRY(load_dict(h, D, &Dp));
+  KSVD_TRY(ensure(h, B_G, (size_t)h->Kp * h->Kp, &G));
+  KSVD_TRY(ensure(h, B_CLEARED, 1, &cd));
+  KSVD_TRY(gram_padded(h, Dp, G));
+  KSVD_TRY(run_clear(h, Dp, G, X, N, cd));
+  KSVD_TRY(store_dict(h, Dp, D));
+  if (cleared) {
+    KSVD_CK(h, cudaMemcpyAsync(cleared, cd, sizeof(int32_t), cudaMemcpyDeviceToHost, h->stream));
+    KSVD_CK(h, cudaStreamSynchronize(h->stream));
+    return check_dev_err(h);
+  }
+  return KSVD_OK;
+}
+
+ksvd_status ksvd_iterate(ksvd_handle* h, float* D, const float* X, int64_t N, int32_t iters,
+                         const int32_t* perms, int32_t* idx, float* coef, int32_t* nnz,
+                         double* rmse) {
+  if (!h || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || N < 1 ||
+      iters < 0)
+    return KSVD_ERR_INVALID_ARGUMENT;
+  if (iters > 1024) return fail(h, KSVD_ERR_UNSUPPORTED, "at most 1024 iterations per call%s");
+  if ((int64_t)N * h->p.T > 0x7fffffffLL)
+    return fail(h, KSVD_ERR_UNSUPPORTED, "N*T must stay below 2^31%s");
+  const int Kp = h->Kp;
+  float *Dp = nullptr, *G = nullptr, *A0 = nullptr;
+  double* rd = nullptr;
+  int32_t *pd = nullptr, *cd = nullptr;
+  KSVD_TRY(load_dict(h, D, &Dp));
+  KSVD_TRY(ensure(h, B_G, (size_t)Kp * Kp, &G));
+  KSVD_TRY(ensure(h, B_A0, (size_t)Kp * N, &A0));
+  KSVD_TRY(ensure(h, B_RMSE, 1024, &rd));
+  KSVD_TRY(ensure(h, B_CLEARED, 1, &cd));
+  if (iters > 0) KSVD_TRY(upload_perm(h, perms, iters, &pd));
+  KSVD_CK(h, launch_normcols(Dp, h->p.n, h->p.K, h->stream));         // KSVD.cu:57
+  KSVD_TRY(gram_padded(h, Dp, G));                                     // KSVD.cu:64
+  for (int32_t it = 0; it < iters; ++it) {
+    KSVD_TRY(dtx_padded(h, Dp, X, N, A0));                             // OMP.cu:44
+    KSVD_TRY(run_omp(h, G, A0, N, nullptr, nullptr, idx, coef, nnz));  // OMP.cu:55
+    KSVD_TRY(run_update(h, Dp, X, N, idx, coef, nnz, pd + (size_t)it * h->p.K));  // KSVD.cu:97-114
+    KSVD_TRY(run_error(h, Dp, X, N, idx, coef, nnz, rd + it));        // KSVD.cu:119
+    KSVD_TRY(gram_padded(h, Dp, G));                                   // G of the updated D
+    KSVD_TRY(run_clear(h, Dp, G, X, N, cd));                           // KSVD.cu:126
+  }
+  KSVD_TRY(store_dict(h, Dp, D));
+  if (rmse && iters > 0)
+    KSVD_CK(h, cudaMemcpyAsync(rmse, rd, sizeof(double) * iters, cudaMemcpyDeviceToHost,
+                               h->stream));
+  KSVD_CK(h, cudaStreamSynchronize(h->stream));
+  collect_stage_times(h);
+  return check_dev_err(h);
+}
+
+ksvd_status ksvd_iterate_host(ksvd_handle* h, float* D, const float* X, int64_t N, int32_t iters,
+                              const int32_t* perms, int32_t* idx, float* coef, int32_t* nnz,
+                              double* rmse) {
+  if (!h || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || N < 1)
+    return KSVD_ERR_INVALID_ARGUMENT;
+  const int n = h->p.n, K = h->p.K, T = h->p.T;
+  float *dX = nullptr, *dD = nullptr, *dC = nullptr;
+  int32_t *dI = nullptr, *dN = nullptr;
+  KSVD_TRY(ensure(h, B_HX, (size_t)n * N, &dX));
+  KSVD_TRY(ensure(h, B_HD, (size_t)n * K, &dD));
+  KSVD_TRY(ensure(h, B_HIDX, (size_t)N * T, &dI));
+  KSVD_TRY(ensure(h, B_HCOEF, (size_t)N * T, &dC));
+  KSVD_TRY(ensure(h, B_HNNZ, (size_t)N, &dN));
+  KSVD_CK(h, cudaMemcpyAsync(dX, X, sizeof(float) * (size_t)n * N, cudaMemcpyHostToDevice, h->stream));
+  KSVD_CK(h, cudaMemcpyAsync(dD, D, sizeof(float) * (size_t)n * K, cudaMemcpyHostToDevice, h->stream));
+  KSVD_TRY(ksvd_iterate(h, dD, dX, N, iters, perms, dI, dC, dN, rmse));
+  KSVD_CK(h, cudaMemcpyAsync(D, dD, sizeof(float) * (size_t)n * K, cudaMemcpyDeviceToHost, h->stream));
+  KSVD_CK(h, cudaMemcpyAsync(idx, dI, sizeof(int32_t) * (size_t)N * T, cudaMemcpyDeviceToHost, h->stream));
+  KSVD_CK(h, cudaMemcpyAsync(coef, dC, sizeof(float) * (size_t)N * T, cudaMemcpyDeviceToHost, h->stream));
+  KSVD_CK(h, cudaMemcpyAsync(nnz, dN, sizeof(int32_t) * (size_t)N, cudaMemcpyDeviceToHost, h->stream));
+  KSVD_CK(h, cudaStreamSynchronize(h->stream));
+  return KSVD_OK;
+}
+
+ksvd_status ksvd_dense_gamma(ksvd_handle* h, int64_t N, const int32_t* idx, const float* coef,
+                             const int32_t* nnz, float* gamma) {
+  if (!h || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || bad_ptr(gamma) || N < 0)
+    return KSVD_ERR_INVALID_ARGUMENT;
+  KSVD_CK(h, launch_dense_gamma(idx, coef, nnz, N, h->p.T, h->p.K, gamma, h->stream));
+  return KSVD_OK;
+}
+
+}  // extern "C"

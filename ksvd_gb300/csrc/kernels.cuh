@@ -1,0 +1,125 @@
+// kernels.cuh -- host launchers of the device kernels (internal interface of libksvd_gb300).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ksvd {
+
+// ---- GEMM (gemm_simt.cu) --------------------------------------------------------------------
+// C[s*ldc + k] = sum_{r<inner} A[k*lda + r] * B[s*ldb + r] for k < M_store, s < N_store, where
+// rows k >= M_load of A and rows s >= N_load of B read as zero (zero padding of the outputs).
+cudaError_t launch_gemm_tn_f32(const float* A, int64_t lda, const float* B, int64_t ldb, float* C,
+                               int64_t ldc, int M_load, int M_store, int64_t N_load,
+                               int64_t N_store, int inner, cudaStream_t st);
+
+// ---- tensor-core GEMM (gemm_tc.cu) ------------------------------------------------------------
+// Mixed precision C = A'B with A, B given as BF16 hi (+ optional lo) parts, FP32 accumulation
+// in TMEM.  Returns cudaErrorNotSupported when the shape is outside the kernel's tiling.
+struct TcOperand {
+  const uint16_t* hi;   // bf16 bits, rows of `inner` contiguous elements, leading dim ld
+  const uint16_t* lo;   // nullable: residual part for the split product
+  int64_t ld;           // elements
+  int64_t rows;         // rows available (multiple of the tile)
+};
+cudaError_t launch_gemm_tn_bf16(const TcOperand& A, const TcOperand& B, float* C, int64_t ldc,
+                                int M, int64_t Ncols, int inner, int passes, cudaStream_t st);
+// hi/lo split of an FP32 matrix stored as `rows` rows of `inner` contiguous floats (ld_in),
+// written with leading dimension ld_out (zero padded to ld_out and to rows_out).
+cudaError_t launch_split_bf16(const float* in, int64_t ld_in, int64_t rows, int inner,
+                              uint16_t* hi, uint16_t* lo, int64_t ld_out, int64_t rows_out,
+                              cudaStream_t st);
+
+// ---- Batch-OMP (omp.cu) -------------------------------------------------------------------------
+// Atom-dimension padding used by every internal buffer: 128, 256, 512 or 1024 (K <= 1024).
+int omp_padded_k(int K);
+// G: Kp x Kp column-major (ldg >= Kp), zero padded; A0: Kp x N column-major (lda >= Kp), zero
+// padded, with Kp = omp_padded_k(K).  T <= 64.
+cudaError_t launch_omp(const float* G, int64_t ldg, const float* A0, int64_t lda, int K,
+                       int64_t N, int T, const float* xnorm2, const float* eps2, int32_t* idx,
+                       float* coef, int32_t* nnz, int* dev_err, cudaStream_t st);
+
+// ---- misc (misc.cu) ---------------------------------------------------------------------------
+cudaError_t launch_normcols(float* D, int n, int K, cudaStream_t st);
+// copy an n x K column-major matrix into an n x Kp buffer (zero columns K..Kp-1)
+cudaError_t launch_copy_pad_cols(const float* src, int n, int K, float* dst, int Kp,
+                                 cudaStream_t st);
+cudaError_t launch_col_norm2(const float* X, int n, int64_t N, float* out, cudaStream_t st);
+cudaError_t launch_dense_gamma(const int32_t* idx, const float* coef, const int32_t* nnz,
+                               int64_t N, int T, int K, float* gamma, cudaStream_t st);
+cudaError_t launch_copy_matrix(const float* src, int64_t ld_src, float* dst, int64_t ld_dst,
+                               int rows, int64_t cols, cudaStream_t st);
+
+// ---- dictionary update (update.cu) ------------------------------------------------------------
+struct UpdateArgs {
+  int n, K, Kp, T;
+  int64_t N;
+  const float* X;        // n x N
+  float* D;              // n x Kp (current dictionary, updated in place)
+  const int32_t* idx;    // N x T
+  float* coef;           // N x T (updated in place)
+  const int32_t* nnz;    // N
+  const int32_t* perm;   // K
+  int max_signals;
+  // workspace
+  int32_t* list;         // total entries (signal*T + slot), per-atom ascending signal order
+  int64_t* start;        // Kp + 1
+  int32_t* block_hist;   // nblk x Kp
+  float* Y;              // n x Kp
+  float* gn2;            // Kp
+  float* C;              // Kp x Kp co-occurrence, C(i,j) = sum_s Gamma(i,s) Gamma(j,s)
+  float* avec;           // n (atom accumulator, zero between atoms)
+  float* aD;             // Kp
+  float* part;           // nctas x 4 scratch
+  int32_t* unused;       // N
+  int32_t* bitmap;       // N
+  int32_t* replaced;     // Kp
+  int64_t* counter;      // 1
+  int32_t* usecount;     // Kp
+  unsigned int* barrier; // 2 words
+  int* dev_err;
+};
+cudaError_t launch_update_prepare(const UpdateArgs& a, cudaStream_t st);
+cudaError_t launch_update_sweep(const UpdateArgs& a, cudaStream_t st);
+int64_t update_block_count(int64_t N);
+int update_sweep_ctas();
+
+// ---- error + clearDict (clear.cu) -------------------------------------------------------------
+struct ErrorArgs {
+  int n, K, Kp, T;
+  int64_t N;
+  const float* X;
+  const float* D;        // n x Kp
+  const int32_t* idx;
+  const float* coef;
+  const int32_t* nnz;
+  const int32_t* bitmap; // nullable
+  float* err;            // N, masked error
+  double* part_sum;      // per error block
+  float* bucket_val;     // per error block: max masked error
+  int64_t* bucket_idx;   // per error block: its signal (lowest on ties)
+  double* rmse_out;      // device scalar
+};
+int64_t error_block_count(int64_t N);
+cudaError_t launch_error(const ErrorArgs& a, cudaStream_t st);
+
+struct ClearArgs {
+  int n, K, Kp;
+  int64_t N;
+  const float* X;
+  float* D;              // n x Kp
+  float* G;              // Kp x Kp, kept equal to D'D
+  const int32_t* usecount;   // signals with gamma^2 > 1e-7 per atom (from the sweep)
+  const int32_t* replaced;
+  float* err;
+  float* bucket_val;
+  int64_t* bucket_idx;
+  int64_t nbuckets;
+  float mu_thresh;
+  int use_thresh;
+  int32_t* cleared;      // device scalar
+};
+// m, mi: Kp scratch floats / ints (per-column largest off-diagonal G^2 and its row)
+cudaError_t launch_clear_dict(const ClearArgs& a, float* m, int* mi, cudaStream_t st);
+
+}  // namespace ksvd

@@ -1,0 +1,266 @@
+// omp.cu -- Batch-OMP (Rubinstein, Zibulevsky & Elad, CS-2008-08) on the GPU: one warp per
+// signal, the K correlations of the signal held in registers (K/32 per lane), the incremental
+// Cholesky factor of G restricted to the support in shared memory (one (TMAX) x (TMAX+1) tile
+// per warp, padded against bank conflicts), and warp-shuffle argmax / reductions.
+//
+// Per step it does what the reference's parOMP does per thread (OMP.cu:254-405):
+//   p = argmax |alpha| (first maximum, maxabs OMP.cu:201-213); stop if p is already selected or
+//   alpha_p^2 < 1e-14 (OMP.cu:292,304); new row w of L from L w = G(I,p) (OMP.cu:321-326),
+//   L_tt = sqrt(1 - ||w||^2), stop if <= 1e-14 (OMP.cu:329-335); forward/backward solves for the
+//   coefficients (OMP.cu:347-357); alpha = alpha0 - G(:,I) gamma (addMul, OMP.cu:365-371).
+// GPU-specific choices: the forward solve is incremental (only the new entry of y = L^-1
+// alpha0_I is computed; the earlier entries do not change), the triangular solves run as
+// column sweeps across the lanes that own the support slots, the final alpha update after the
+// last atom is skipped (it is never read), and a failed pivot test does not add the atom.
+// alpha0 is streamed once (evict-first loads); G stays L2-resident.
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace ksvd {
+namespace {
+
+constexpr int kOmpWarps = 8;
+
+template <int SPL>
+__device__ __forceinline__ float pick(const float (&a)[SPL], int j) {
+  if constexpr (SPL == 1) return a[0];
+  else return j == 0 ? a[0] : a[1];
+}
+template <int SPL>
+__device__ __forceinline__ int pick(const int (&a)[SPL], int j) {
+  if constexpr (SPL == 1) return a[0];
+  else return j == 0 ? a[0] : a[1];
+}
+template <int SPL, typename V>
+__device__ __forceinline__ void put(V (&a)[SPL], int j, V v) {
+  if constexpr (SPL == 1) a[0] = v;
+  else { if (j == 0) a[0] = v; else a[1] = v; }
+}
+
+template <int KPL, int TMAX>
+__global__ void __launch_bounds__(kOmpWarps * 32, 2)
+omp_kernel(const float* __restrict__ G, int64_t ldg, const float* __restrict__ A0, int64_t lda,
+           int K, int64_t N, int T, const float* __restrict__ xnorm2,
+           const float* __restrict__ eps2, int32_t* __restrict__ idx_out,
+           float* __restrict__ coef_out, int32_t* __restrict__ nnz_out, int* __restrict__ dev_err) {
+  constexpr int M4 = KPL / 4;    // float4 groups per lane; lane owns rows 128*m + 4*lane + q
+  constexpr int SPL = TMAX / 32; // support slots per lane; lane owns slots lane + 32*j
+  constexpr int LS = TMAX + 1;   // row stride of L in shared memory
+  extern __shared__ float smem[];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  float* L = smem + (size_t)wib * TMAX * LS;
+  const int64_t warps_total = (int64_t)gridDim.x * kOmpWarps;
+  bool numeric_bad = false;
+
+  for (int64_t s = (int64_t)blockIdx.x * kOmpWarps + wib; s < N; s += warps_total) {
+    float a0[M4][4], al[M4][4];
+    const float* a0p = A0 + s * lda + 4 * lane;
+#pragma unroll
+    for (int m = 0; m < M4; ++m) {
+      float4 v = __ldcs(reinterpret_cast<const float4*>(a0p + 128 * m));
+      a0[m][0] = v.x; a0[m][1] = v.y; a0[m][2] = v.z; a0[m][3] = v.w;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) al[m][q] = a0[m][q];
+    }
+    int ind[SPL];
+    float y[SPL], c[SPL];
+#pragma unroll
+    for (int j = 0; j < SPL; ++j) { ind[j] = -1; y[j] = 0.f; c[j] = 0.f; }
+
+    const bool emode = eps2 != nullptr;
+    const float e2 = emode ? eps2[s] : 0.f;
+    const float xn2 = emode ? xnorm2[s] : 0.f;
+    float r2 = xn2;
+    int i = 0;
+    while (i < T) {
+      if (emode && r2 <= e2) break;
+      // ---- argmax |alpha| (first maximum) with alpha_p and alpha0_p as payload
+      float bv = -1.f, bal = 0.f, ba0 = 0.f;
+      int bk = 0x7fffffff;
+#pragma unroll
+      for (int m = 0; m < M4; ++m)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int k = 128 * m + 4 * lane + q;
+          const float v = al[m][q] * al[m][q];
+          if (k < K && v > bv) { bv = v; bk = k; bal = al[m][q]; ba0 = a0[m][q]; }
+        }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float ov = __shfl_xor_sync(KSVD_FULL_MASK, bv, o);
+        const int ok = __shfl_xor_sync(KSVD_FULL_MASK, bk, o);
+        const float oal = __shfl_xor_sync(KSVD_FULL_MASK, bal, o);
+        const float oa0 = __shfl_xor_sync(KSVD_FULL_MASK, ba0, o);
+        if (ov > bv || (ov == bv && ok < bk)) { bv = ov; bk = ok; bal = oal; ba0 = oa0; }
+      }
+      if (bk >= K) { numeric_bad = true; break; }   // every |alpha| was NaN
+      const int p = bk;
+      bool dup = false;
+#pragma unroll
+      for (int j = 0; j < SPL; ++j) dup |= (lane + 32 * j < i) && ind[j] == p;
+      if (__any_sync(KSVD_FULL_MASK, dup)) break;
+      if (bal * bal < 1e-14f) break;
+
+      float Lii = 1.f, ynew = ba0;
+      if (i > 0) {
+        // b = G(I, p); forward column sweep solves L w = b, lane q ends with w_q
+        float b[SPL], w[SPL];
+#pragma unroll
+        for (int j = 0; j < SPL; ++j) {
+          const int q = lane + 32 * j;
+          b[j] = q < i ? __ldg(G + (int64_t)ind[j] * ldg + p) : 0.f;
+          w[j] = 0.f;
+        }
+        for (int r = 0; r < i; ++r) {
+          const int rl = r & 31, rj = r >> 5;
+          const float wr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(b, rj), rl) / L[r * LS + r];
+          if (lane == rl) put<SPL>(w, rj, wr);
+#pragma unroll
+          for (int j = 0; j < SPL; ++j) {
+            const int q = lane + 32 * j;
+            if (q > r && q < i) b[j] = fmaf(-L[q * LS + r], wr, b[j]);
+          }
+        }
+        float ss = 0.f, wy = 0.f;
+#pragma unroll
+        for (int j = 0; j < SPL; ++j) {
+          if (lane + 32 * j < i) { ss = fmaf(w[j], w[j], ss); wy = fmaf(w[j], y[j], wy); }
+        }
+        ss = warp_sum(ss);
+        const float l2 = 1.f - ss;
+        if (l2 <= 1e-14f) break;               // pivot test failed: the atom is not added
+        Lii = sqrtf(l2);
+        wy = warp_sum(wy);
+        ynew = (ba0 - wy) / Lii;
+#pragma unroll
+        for (int j = 0; j < SPL; ++j) {
+          const int q = lane + 32 * j;
+          if (q < i) L[i * LS + q] = w[j];
+        }
+      }
+      if (lane == 0) L[i * LS + i] = Lii;
+      if (lane == (i & 31)) { put<SPL>(ind, i >> 5, p); put<SPL>(y, i >> 5, ynew); }
+      ++i;
+      __syncwarp();
+
+      if (emode) {
+        float yy = 0.f;
+#pragma unroll
+        for (int j = 0; j < SPL; ++j)
+          if (lane + 32 * j < i) yy = fmaf(y[j], y[j], yy);
+        r2 = xn2 - warp_sum(yy);
+      }
+      // ---- backward column sweep: L' c = y
+      {
+        float t[SPL];
+#pragma unroll
+        for (int j = 0; j < SPL; ++j) t[j] = y[j];
+        for (int r = i - 1; r >= 0; --r) {
+          const int rl = r & 31, rj = r >> 5;
+          const float cr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(t, rj), rl) / L[r * LS + r];
+          if (lane == rl) put<SPL>(c, rj, cr);
+#pragma unroll
+          for (int j = 0; j < SPL; ++j) {
+            const int q = lane + 32 * j;
+            if (q < r) t[j] = fmaf(-L[r * LS + q], cr, t[j]);
+          }
+        }
+      }
+      // ---- alpha = alpha0 - G(:, I) c   (not needed after the last atom)
+      if (i < T && !(emode && r2 <= e2)) {
+#pragma unroll
+        for (int m = 0; m < M4; ++m)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) al[m][q] = 0.f;
+#pragma unroll 2
+        for (int r = 0; r < i; ++r) {
+          const int rl = r & 31, rj = r >> 5;
+          const float cr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(c, rj), rl);
+          const int col = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(ind, rj), rl);
+          const float* gp = G + (int64_t)col * ldg + 4 * lane;
+#pragma unroll
+          for (int m = 0; m < M4; ++m) {
+            const float4 g = __ldg(reinterpret_cast<const float4*>(gp + 128 * m));
+            al[m][0] = fmaf(g.x, cr, al[m][0]);
+            al[m][1] = fmaf(g.y, cr, al[m][1]);
+            al[m][2] = fmaf(g.z, cr, al[m][2]);
+            al[m][3] = fmaf(g.w, cr, al[m][3]);
+          }
+        }
+#pragma unroll
+        for (int m = 0; m < M4; ++m)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) al[m][q] = a0[m][q] - al[m][q];
+      }
+    }
+    // ---- outputs: slots in selection order, -1 / 0 padding
+#pragma unroll
+    for (int j = 0; j < SPL; ++j) {
+      const int q = lane + 32 * j;
+      if (q < T) {
+        const bool used = q < i;
+        idx_out[s * T + q] = used ? ind[j] : -1;
+        coef_out[s * T + q] = used ? c[j] : 0.f;
+        if (used && !finitef(c[j])) numeric_bad = true;
+      }
+    }
+    if (lane == 0) nnz_out[s] = i;
+  }
+  if (__any_sync(KSVD_FULL_MASK, numeric_bad) && lane == 0) atomicOr(dev_err, kDevErrNumeric);
+}
+
+template <int KPL, int TMAX>
+cudaError_t launch_omp_t(const float* G, int64_t ldg, const float* A0, int64_t lda, int K,
+                         int64_t N, int T, const float* xnorm2, const float* eps2, int32_t* idx,
+                         float* coef, int32_t* nnz, int* dev_err, cudaStream_t st) {
+  const size_t smem = (size_t)kOmpWarps * TMAX * (TMAX + 1) * sizeof(float);
+  auto kern = omp_kernel<KPL, TMAX>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kOmpWarps * 32, smem);
+  if (per_sm < 1) per_sm = 1;
+  int64_t blocks = (N + kOmpWarps - 1) / kOmpWarps;
+  const int64_t cap = (int64_t)sms * per_sm * 8;
+  if (blocks > cap) blocks = cap;
+  kern<<<(unsigned)blocks, kOmpWarps * 32, smem, st>>>(G, ldg, A0, lda, K, N, T, xnorm2, eps2, idx,
+                                                       coef, nnz, dev_err);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+int omp_padded_k(int K) {
+  return K <= 128 ? 128 : K <= 256 ? 256 : K <= 512 ? 512 : 1024;
+}
+
+cudaError_t launch_omp(const float* G, int64_t ldg, const float* A0, int64_t lda, int K,
+                       int64_t N, int T, const float* xnorm2, const float* eps2, int32_t* idx,
+                       float* coef, int32_t* nnz, int* dev_err, cudaStream_t st) {
+  if (N <= 0) return cudaSuccess;
+  if (K < 1 || K > kMaxK || T < 1 || T > kMaxT) return cudaErrorInvalidValue;
+  const int kp = omp_padded_k(K);   // the lanes touch rows [0, kp) of every column
+  if (ldg < kp || lda < kp || (ldg & 3) || (lda & 3)) return cudaErrorInvalidValue;
+#define KSVD_OMP_ARGS G, ldg, A0, lda, K, N, T, xnorm2, eps2, idx, coef, nnz, dev_err, st
+  if (T <= 32) {
+    switch (kp) {
+      case 128: return launch_omp_t<4, 32>(KSVD_OMP_ARGS);
+      case 256: return launch_omp_t<8, 32>(KSVD_OMP_ARGS);
+      case 512: return launch_omp_t<16, 32>(KSVD_OMP_ARGS);
+      default: return launch_omp_t<32, 32>(KSVD_OMP_ARGS);
+    }
+  }
+  switch (kp) {
+    case 128: return launch_omp_t<4, 64>(KSVD_OMP_ARGS);
+    case 256: return launch_omp_t<8, 64>(KSVD_OMP_ARGS);
+    case 512: return launch_omp_t<16, 64>(KSVD_OMP_ARGS);
+    default: return launch_omp_t<32, 64>(KSVD_OMP_ARGS);
+  }
+#undef KSVD_OMP_ARGS
+}
+
+}  // namespace ksvd

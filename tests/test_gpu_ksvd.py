@@ -1,0 +1,290 @@
+"""GPU parity: every stage of libksvd_gb300 (through the C ABI) against the CPU oracle on the same
+seeded inputs.  Tolerances (FP32 GPU vs FP64 oracle):
+  * OMP supports: identical sets on >= 99.9% of signals;
+  * coefficients, dictionary: relative RMSE <= 1e-4;
+  * RMSE per iteration: relative difference <= 1e-4.
+"""
+import numpy as np
+import pytest
+
+from conftest import coef_by_atom, rel_rmse, support_match_vec
+
+pytestmark = pytest.mark.gpu
+
+SUPPORT_MIN = 0.999
+REL_TOL = 1e-4
+
+
+def to_dev(a, cuda):
+    """numpy column-major (rows x cols) -> torch (cols, rows) contiguous float32 on the GPU."""
+    import torch
+
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(a, np.float32).T)).to(cuda)
+
+
+def from_dev(t):
+    """torch (cols, rows) -> numpy column-major (rows x cols) float64."""
+    return np.asfortranarray(t.double().cpu().numpy().T)
+
+
+def problem(n, K, N, T, seed, noise=0.05):
+    rng = np.random.default_rng(seed)
+    D0 = rng.standard_normal((n, K))
+    D0 /= np.linalg.norm(D0, axis=0)
+    X = np.zeros((n, N))
+    for s in range(N):
+        S = rng.choice(K, T, replace=False)
+        X[:, s] = D0[:, S] @ rng.standard_normal(T)
+    X += noise * rng.standard_normal((n, N)) * np.linalg.norm(X, axis=0) / np.sqrt(n)
+    D = X[:, rng.choice(N, K, replace=False)]
+    D /= np.linalg.norm(D, axis=0)
+    return np.asfortranarray(X.astype(np.float32)), np.asfortranarray(D.astype(np.float32))
+
+
+def omp_check(oracle_mod, cuda, n, K, N, T, seed, eps_frac=None):
+    from ksvd_gb300 import Handle
+
+    X, D = problem(n, K, N, T if T < K else max(1, K // 2), seed)
+    h = Handle(n, K, T)
+    Xd, Dd = to_dev(X, cuda), to_dev(D, cuda)
+    eps2 = None
+    X64, D64 = X.astype(np.float64), D.astype(np.float64)
+    G, A0 = oracle_mod.gram(D64), oracle_mod.dtx(D64, X64)
+    if eps_frac is not None:
+        xn2 = np.sum(X64 * X64, 0)
+        e2 = (eps_frac * xn2).astype(np.float32)
+        import torch
+
+        eps2 = torch.from_numpy(e2).to(cuda)
+        ri, rc, rn = oracle_mod.omp(G, A0, T, xnorm2=xn2, eps2=e2.astype(np.float64))
+    else:
+        ri, rc, rn = oracle_mod.omp(G, A0, T)
+    idx, coef, nnz = h.omp(Dd, Xd, eps2=eps2)
+    h.synchronize()
+    gi, gc, gn = idx.cpu().numpy(), coef.cpu().numpy(), nnz.cpu().numpy()
+    match = support_match_vec(gi, gn, ri, rn)
+    assert match >= SUPPORT_MIN, match
+    ok = np.all(np.sort(np.where(np.arange(T) < gn[:, None], gi, 1 << 30), 1) ==
+                np.sort(np.where(np.arange(T) < rn[:, None], ri, 1 << 30), 1), 1) & (gn == rn)
+    ca, cb = coef_by_atom(gi[ok], gc[ok], gn[ok], K), coef_by_atom(ri[ok], rc[ok], rn[ok], K)
+    assert rel_rmse(ca, cb) <= REL_TOL
+    # padding slots
+    ar = np.arange(T)[None, :]
+    assert np.all(gi[ar >= gn[:, None]] == -1) and np.all(gc[ar >= gn[:, None]] == 0)
+    h.close()
+    return gn
+
+
+def test_gram_and_dtx(oracle_mod, cuda):
+    from ksvd_gb300 import Handle
+
+    X, D = problem(64, 200, 1500, 6, 1)
+    h = Handle(64, 200, 6)
+    Xd, Dd = to_dev(X, cuda), to_dev(D, cuda)
+    G = from_dev(h.gram(Dd))
+    A0 = from_dev(h.dtx(Dd, Xd))
+    Gr = oracle_mod.gram(D.astype(np.float64))
+    Ar = oracle_mod.dtx(D.astype(np.float64), X.astype(np.float64))
+    assert rel_rmse(G, Gr) < 1e-6 and rel_rmse(A0, Ar) < 1e-6
+    assert np.max(np.abs(A0 - Ar)) < 1e-4
+
+
+@pytest.mark.parametrize("n,K,N,T,seed", [
+    (64, 256, 6000, 8, 10),      # cfg0 shape
+    (200, 512, 3000, 10, 11),    # cfg1 shape
+    (256, 1024, 2000, 16, 12),   # cfg2 shape
+    (300, 9, 3600, 6, 13),       # the reference's own shape
+    (48, 100, 2000, 5, 14),      # K not a multiple of 128
+    (32, 40, 500, 40, 15),       # T = K (64-slot path)
+    (20, 7, 300, 1, 16),         # T = 1
+])
+def test_omp_matches_oracle(oracle_mod, cuda, n, K, N, T, seed):
+    omp_check(oracle_mod, cuda, n, K, N, T, seed)
+
+
+def test_omp_error_target(oracle_mod, cuda):
+    gn = omp_check(oracle_mod, cuda, 128, 512, 3000, 48, 17, eps_frac=0.02)
+    assert gn.min() < gn.max()          # uneven supports
+
+
+def test_omp_edge_cases(oracle_mod, cuda):
+    import torch
+    from ksvd_gb300 import Handle
+
+    rng = np.random.default_rng(18)
+    Q, _ = np.linalg.qr(rng.standard_normal((32, 32)))
+    X = np.zeros((32, 4), np.float32)
+    X[:, 1] = Q[:, 3] * 2 - Q[:, 7]          # exactly two atoms, T = 5 stops early
+    X[:, 2] = Q[:, 0]
+    X[:, 3] = rng.standard_normal(32)
+    h = Handle(32, 32, 5)
+    idx, coef, nnz = h.omp(to_dev(Q, cuda), to_dev(X, cuda))
+    h.synchronize()
+    nnz = nnz.cpu().numpy()
+    idx = idx.cpu().numpy()
+    coef = coef.cpu().numpy()
+    assert nnz[0] == 0                        # zero signal
+    assert nnz[1] == 2 and set(idx[1, :2]) == {3, 7}
+    np.testing.assert_allclose(sorted(coef[1, :2]), [-1, 2], atol=1e-5)
+    assert nnz[2] == 1 and idx[2, 0] == 0
+    assert nnz[3] == 5
+    # a single signal
+    idx1, coef1, nnz1 = h.omp(to_dev(Q, cuda), to_dev(X[:, 3:4], cuda))
+    h.synchronize()
+    assert np.array_equal(idx1.cpu().numpy()[0], idx[3])
+
+
+def code_from_oracle(oracle_mod, X, D, T):
+    X64, D64 = X.astype(np.float64), D.astype(np.float64)
+    return oracle_mod.omp(oracle_mod.gram(D64), oracle_mod.dtx(D64, X64), T)
+
+
+@pytest.mark.parametrize("n,K,N,T,seed,unused_atom", [
+    (64, 256, 8000, 8, 20, False),
+    (256, 1024, 20000, 16, 21, False),
+    (40, 64, 3000, 4, 22, True),
+])
+def test_update_matches_oracle(oracle_mod, cuda, n, K, N, T, seed, unused_atom):
+    import torch
+    from ksvd_gb300 import Handle
+
+    X, D = problem(n, K, N, T, seed)
+    if unused_atom:
+        P = np.linalg.svd(X.astype(np.float64), full_matrices=True)[0]
+        X = np.asfortranarray((X - np.outer(P[:, -1], P[:, -1] @ X)).astype(np.float32))
+        D[:, 5] = P[:, -1]
+    idx, coef, nnz = code_from_oracle(oracle_mod, X, D, T)
+    if unused_atom:
+        assert not np.any((idx == 5) & (np.arange(T)[None, :] < nnz[:, None]))
+    perm = np.random.default_rng(seed).permutation(K).astype(np.int32)
+    coef32 = coef.astype(np.float32)
+    Dr, cr, st = oracle_mod.update(X.astype(np.float64), D.astype(np.float64), idx,
+                                   coef32.astype(np.float64), nnz, perm)
+    h = Handle(n, K, T)
+    Dd = to_dev(D, cuda)
+    cd = torch.from_numpy(coef32).to(cuda)
+    h.update_dictionary(Dd, to_dev(X, cuda), torch.from_numpy(idx).to(cuda), cd,
+                        torch.from_numpy(nnz).to(cuda), perm)
+    h.synchronize()
+    assert rel_rmse(from_dev(Dd), Dr) <= REL_TOL
+    assert rel_rmse(cd.cpu().numpy(), cr) <= REL_TOL
+    if unused_atom:
+        assert st["replaced"][5] == 1
+        np.testing.assert_allclose(from_dev(Dd)[:, 5], Dr[:, 5], atol=1e-5)
+    h.close()
+
+
+def test_error_and_clear_match_oracle(oracle_mod, cuda):
+    import torch
+    from ksvd_gb300 import Handle
+
+    n, K, N, T = 48, 96, 4000, 4
+    X, D = problem(n, K, N, T, 30)
+    D[:, 40] = D[:, 10] + 0.05 * np.random.default_rng(30).standard_normal(n)
+    D /= np.linalg.norm(D, axis=0)
+    idx, coef, nnz = code_from_oracle(oracle_mod, X, D, T)
+    perm = np.arange(K, dtype=np.int32)
+    X64 = X.astype(np.float64)
+    Dr, cr, st = oracle_mod.update(X64, D.astype(np.float64), idx, coef.astype(np.float32)
+                                   .astype(np.float64), nnz, perm)
+    rr, er = oracle_mod.error(X64, Dr, idx, cr, nnz, st["bitmap"])
+    Dc, ec, cleared_r = oracle_mod.cleardict(X64, Dr, idx, cr, nnz, st["replaced"], er)
+
+    h = Handle(n, K, T)
+    Dd, Xd = to_dev(D, cuda), to_dev(X, cuda)
+    idd, nnd = torch.from_numpy(idx).to(cuda), torch.from_numpy(nnz).to(cuda)
+    cd = torch.from_numpy(coef.astype(np.float32)).to(cuda)
+    h.update_dictionary(Dd, Xd, idd, cd, nnd, perm)
+    r, e = h.error(Dd, Xd, idd, cd, nnd, want_err=True)
+    assert abs(r - rr) / rr <= REL_TOL
+    assert rel_rmse(e.cpu().numpy(), er) <= REL_TOL
+    cleared = h.clear_dict(Dd, Xd, idd, cd, nnd)
+    assert cleared == cleared_r and cleared >= 1
+    assert rel_rmse(from_dev(Dd), Dc) <= REL_TOL
+    h.close()
+
+
+def test_stage_order_is_enforced(cuda):
+    import torch
+    from ksvd_gb300 import Handle, KsvdError
+
+    X, D = problem(16, 20, 100, 2, 31)
+    h = Handle(16, 20, 2)
+    Dd, Xd = to_dev(D, cuda), to_dev(X, cuda)
+    idx, coef, nnz = h.omp(Dd, Xd)
+    with pytest.raises(KsvdError) as ei:
+        h.clear_dict(Dd, Xd, idx, coef, nnz)
+    assert ei.value.status_name == "KSVD_ERR_STATE"
+
+
+@pytest.mark.parametrize("cfg,N,iters", [("cfg0", 4000, 3), ("ref", 3600, 4)])
+def test_iterate_matches_oracle(oracle_mod, cuda, cfg, N, iters):
+    from ksvd_gb300 import Handle, datagen, random_permutation
+
+    p = datagen.make_problem(cfg, N=N)
+    c = p["cfg"]
+    X, D = p["X"], p["D"]
+    perms = np.stack([random_permutation(7, it, c.K) for it in range(iters)])
+    Dr, ri, rc, rn, rr = oracle_mod.ksvd(X.astype(np.float64), D.astype(np.float64), c.T, iters,
+                                         perms)
+    h = Handle(c.n, c.K, c.T)
+    Dd = to_dev(D, cuda)
+    idx, coef, nnz, rmse = h.iterate(Dd, to_dev(X, cuda), iters, perms)
+    np.testing.assert_allclose(rmse, rr, rtol=REL_TOL)
+    gi, gn = idx.cpu().numpy(), nnz.cpu().numpy()
+    assert support_match_vec(gi, gn, ri, rn) >= SUPPORT_MIN
+    assert rel_rmse(from_dev(Dd), Dr) <= 10 * REL_TOL
+    h.close()
+
+
+def test_iterate_host_matches_device(oracle_mod, cuda):
+    from ksvd_gb300 import Handle, datagen, random_permutation
+
+    p = datagen.make_problem("cfg0", N=2000)
+    X, D = p["X"], p["D"]
+    perms = np.stack([random_permutation(3, it, 256) for it in range(2)])
+    h = Handle(64, 256, 8)
+    Dh, ih, ch, nh, rh = h.iterate_host(D, X, 2, perms)
+    Dd = to_dev(D, cuda)
+    idx, coef, nnz, rd = h.iterate(Dd, to_dev(X, cuda), 2, perms)
+    np.testing.assert_array_equal(rh, rd)
+    np.testing.assert_array_equal(ih, idx.cpu().numpy())
+    np.testing.assert_array_equal(Dh, from_dev(Dd).astype(np.float32))
+
+
+def test_full_size_properties(oracle_mod, cuda):
+    """At the headline size (n=256, K=1024, N=1,000,000, T=16): one iteration through the C ABI,
+    then size-independent checks: sorted-support validity, unit-norm atoms, the RMSE reported by
+    the library equals the RMSE recomputed from its outputs, and Batch-OMP on a 2,000-signal
+    sample equals the oracle's."""
+    import torch
+    from ksvd_gb300 import Handle, datagen
+
+    p = datagen.make_problem("cfg2", device="cuda")
+    X, D = p["X"], p["D"]
+    D0 = D.clone()
+    h = Handle(256, 1024, 16)
+    idx, coef, nnz, rmse = h.iterate(D, X, 1)
+    assert int(nnz.min()) >= 1 and int(nnz.max()) <= 16
+    srt = torch.sort(idx.long(), 1).values
+    assert bool(((srt[:, 1:] != srt[:, :-1]) | (srt[:, 1:] < 0)).all())   # distinct atoms
+    assert float((D.norm(dim=1) - 1).abs().max()) < 1e-4
+    # RMSE recomputed from the outputs (chunked, FP64 accumulation)
+    tot = 0.0
+    for s0 in range(0, X.shape[0], 1 << 17):
+        s1 = min(X.shape[0], s0 + (1 << 17))
+        li = idx[s0:s1].long().clamp(min=0)
+        rec = torch.einsum("stn,st->sn", D[li], coef[s0:s1])
+        tot += float(((X[s0:s1] - rec).double() ** 2).sum())
+    assert abs(np.sqrt(tot / X.numel()) - rmse[0]) / rmse[0] < 1e-4
+    # OMP sample against the oracle (the dictionary the first iteration coded with)
+    samp = torch.arange(0, X.shape[0], X.shape[0] // 2000, device=X.device)[:2000]
+    Xs = X[samp].contiguous()
+    Dn = D0 / D0.norm(dim=1, keepdim=True)
+    i2, c2, n2 = h.omp(Dn.contiguous(), Xs)
+    h.synchronize()
+    Xs64 = np.asfortranarray(Xs.double().cpu().numpy().T)
+    Dn64 = np.asfortranarray(Dn.double().cpu().numpy().T)
+    ri, rc, rn = oracle_mod.omp(oracle_mod.gram(Dn64), oracle_mod.dtx(Dn64, Xs64), 16)
+    assert support_match_vec(i2.cpu().numpy(), n2.cpu().numpy(), ri, rn) >= SUPPORT_MIN
+    h.close()
