@@ -29,9 +29,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-KERNELS_PER_CALL = 3          # pad copy, normcols, Gram before the first iteration
-KERNELS_PER_ITER = 14         # D'X, OMP, 6 list/precompute kernels, sweep, error, RMSE, Gram,
-#                               coherence, clearDict
+# kernels launched by one ksvd_iterate call: before the first iteration (pad copy, normcols,
+# Gram; mixed adds the D split for the Gram and the X split) and per iteration (D'X, OMP, six
+# list/precompute kernels, sweep, error, RMSE, Gram, coherence, clearDict; mixed adds two
+# dictionary splits)
+KERNELS_PER_CALL = {"fp32": 3, "mixed": 5}
+KERNELS_PER_ITER = {"fp32": 14, "mixed": 16}
 
 
 def peaks():
@@ -203,6 +206,8 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "mixed"])
     ap.add_argument("--config", default="cfg2")
     ap.add_argument("--cpu-sample", type=int, default=50000)
+    ap.add_argument("--signals", type=int, default=None,
+                    help="override N (smaller cases for profiler captures)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
@@ -211,6 +216,10 @@ def main():
     from ksvd_gb300 import datagen
 
     cfg = datagen.CONFIGS[args.config]
+    if args.signals:
+        import dataclasses
+
+        cfg = dataclasses.replace(cfg, N=int(args.signals))
     if args.impl == "reference":
         return run_reference(args, cfg)
 
@@ -232,16 +241,14 @@ def main():
     if rank == 0 and ws == 1 and not args.no_cpu:
         cpu = cpu_baseline(cfg, args.cpu_sample)
 
-    prob = datagen.make_problem(cfg, seed=datagen.SEED_BASE + cfg.index + 1000 * rank,
-                                device="cuda")
+    prob = datagen.make_problem(cfg, N=args.signals,
+                                seed=datagen.SEED_BASE + cfg.index + 1000 * rank, device="cuda")
     X, D = prob["X"], prob["D"]
     N = X.shape[0]
     h = Handle(cfg.n, cfg.K, cfg.T, precision=args.precision, profile=True)
     idx, coef, nnz = h._code(N, dev)
     out = (idx, coef, nnz)
-    rms = []
-    for _ in range(args.warmup):
-        rms += list(h.iterate(D, X, 1, out=out)[3])
+    rms = list(h.iterate(D, X, args.warmup, out=out)[3])
     h.stage_times(reset=True)
     sampler = ClockSampler(local)
     if dist:
@@ -252,8 +259,7 @@ def main():
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t_wall = time.perf_counter()
     e0.record(stream)
-    for _ in range(args.steps):
-        rms += list(h.iterate(D, X, 1, out=out)[3])
+    rms += list(h.iterate(D, X, args.steps, out=out)[3])      # K steps = K iterations
     e1.record(stream)
     torch.cuda.synchronize()
     t_wall = time.perf_counter() - t_wall
@@ -266,7 +272,7 @@ def main():
     st = h.stage_times()
     value = ws * args.steps / (ms / 1e3)
 
-    # dominant stage and its roofline
+    # dominant stage and its roofline (per-launch device time from events on the kernels' stream)
     pk = peaks()
     per = {k: (v[0] / max(v[1], 1), v[1]) for k, v in st.items() if v[1] > 0}
     dom = max(per, key=lambda k: per[k][0] * per[k][1])
@@ -333,7 +339,8 @@ def main():
             "roofline": roof,
             "cpu_baseline": cpu,
             "e2e": e2e,
-            "gpu_launches": args.steps * (KERNELS_PER_CALL + KERNELS_PER_ITER),
+            "gpu_launches": KERNELS_PER_CALL[args.precision] +
+            args.steps * KERNELS_PER_ITER[args.precision],
             "clocks": clocks,
             "rmse_last": rms[-1] if rms else None,
             "wall_s_timed": t_wall,

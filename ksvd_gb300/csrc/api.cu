@@ -33,6 +33,9 @@ struct ksvd_handle {
   int64_t update_N = -1;
   int64_t error_N = -1;
   int64_t perm_draws = 0;
+  // BF16 hi/lo copy of X for the mixed path (valid for one call: X may change between calls)
+  const float* xsplit_src = nullptr;
+  int64_t xsplit_N = -1;
   // stage profiling (KSVD_FLAG_PROFILE)
   struct Pending { int stage; cudaEvent_t a, b; };
   std::vector<cudaEvent_t> ev_pool;
@@ -49,7 +52,7 @@ enum BufId {
   B_DPAD, B_G, B_A0, B_XN2, B_LIST, B_START, B_BHIST, B_Y, B_GN2, B_C, B_AVEC, B_AD, B_PART,
   B_UNUSED, B_BITMAP, B_REPLACED, B_COUNTER, B_USE, B_BARRIER, B_ERR, B_PSUM, B_BVAL, B_BIDX,
   B_RMSE, B_M, B_MI, B_CLEARED, B_DEVERR, B_PERM, B_GPAD_IN, B_HX, B_HD, B_HIDX, B_HCOEF, B_HNNZ,
-  B_COUNT
+  B_XHI, B_XLO, B_DHI, B_DLO, B_P, B_COUNT
 };
 
 ksvd_status fail(ksvd_handle* h, ksvd_status s, const char* fmt, const char* detail = nullptr) {
@@ -185,18 +188,72 @@ ksvd_status store_dict(ksvd_handle* h, const float* Dp, float* D) {
   return KSVD_OK;
 }
 
+int64_t bf16_ld(int n) { return round_up(n, 8); }
+
+bool mixed(const ksvd_handle* h) { return h->p.precision == KSVD_PREC_MIXED; }
+
+// BF16 hi/lo parts of the padded working dictionary (Kp rows of n).
+ksvd_status split_dict(ksvd_handle* h, const float* Dp, TcOperand* op) {
+  const int n = h->p.n, Kp = h->Kp;
+  const int64_t ld = bf16_ld(n);
+  uint16_t *hi = nullptr, *lo = nullptr;
+  KSVD_TRY(ensure(h, B_DHI, (size_t)Kp * ld, &hi));
+  KSVD_TRY(ensure(h, B_DLO, (size_t)Kp * ld, &lo));
+  KSVD_CK(h, launch_split_bf16(Dp, n, Kp, n, hi, lo, ld, Kp, h->stream));
+  op->hi = hi; op->lo = lo; op->ld = ld; op->rows = Kp;
+  return KSVD_OK;
+}
+
+// BF16 hi/lo parts of X (N rows of n); made once per call and reused by every iteration.
+ksvd_status split_signals(ksvd_handle* h, const float* X, int64_t N, TcOperand* op) {
+  const int n = h->p.n;
+  const int64_t ld = bf16_ld(n);
+  uint16_t *hi = nullptr, *lo = nullptr;
+  KSVD_TRY(ensure(h, B_XHI, (size_t)N * ld, &hi));
+  KSVD_TRY(ensure(h, B_XLO, (size_t)N * ld, &lo));
+  if (h->xsplit_src != X || h->xsplit_N != N) {
+    StageScope sc(h, KSVD_STAGE_DTX);
+    KSVD_CK(h, launch_split_bf16(X, n, N, n, hi, lo, ld, N, h->stream));
+    h->xsplit_src = X;
+    h->xsplit_N = N;
+  }
+  op->hi = hi; op->lo = lo; op->ld = ld; op->rows = N;
+  return KSVD_OK;
+}
+
+// Forget the cached X split (called at the end of every public call).
+void drop_xsplit(ksvd_handle* h) { h->xsplit_src = nullptr; h->xsplit_N = -1; }
+
 // G = D'D for the padded working dictionary (Kp x Kp, zero padded)
 ksvd_status gram_padded(ksvd_handle* h, const float* Dp, float* G) {
   StageScope sc(h, KSVD_STAGE_GRAM);
   const int n = h->p.n, K = h->p.K, Kp = h->Kp;
+  if (mixed(h)) {
+    TcOperand d;
+    int* de = nullptr;
+    KSVD_TRY(ensure(h, B_DEVERR, 1, &de));
+    KSVD_TRY(split_dict(h, Dp, &d));
+    KSVD_CK(h, launch_gemm_tn_bf16(d, d, G, Kp, Kp, Kp, n, 3, de, h->stream));
+    return KSVD_OK;
+  }
   KSVD_CK(h, launch_gemm_tn_f32(Dp, n, Dp, n, G, Kp, K, Kp, K, Kp, n, h->stream));
   return KSVD_OK;
 }
 
 // alpha0 = D'X into the Kp x N buffer (rows K..Kp-1 zero)
 ksvd_status dtx_padded(ksvd_handle* h, const float* Dp, const float* X, int64_t N, float* A0) {
-  StageScope sc(h, KSVD_STAGE_DTX);
   const int n = h->p.n, K = h->p.K, Kp = h->Kp;
+  if (mixed(h)) {
+    TcOperand d, x;
+    int* de = nullptr;
+    KSVD_TRY(ensure(h, B_DEVERR, 1, &de));
+    KSVD_TRY(split_signals(h, X, N, &x));
+    StageScope sc(h, KSVD_STAGE_DTX);
+    KSVD_TRY(split_dict(h, Dp, &d));
+    KSVD_CK(h, launch_gemm_tn_bf16(d, x, A0, Kp, Kp, N, n, 3, de, h->stream));
+    return KSVD_OK;
+  }
+  StageScope sc(h, KSVD_STAGE_DTX);
   KSVD_CK(h, launch_gemm_tn_f32(Dp, n, X, n, A0, Kp, K, Kp, N, N, n, h->stream));
   return KSVD_OK;
 }
@@ -227,8 +284,10 @@ ksvd_status update_ws(ksvd_handle* h, int64_t N, UpdateArgs& u) {
   KSVD_TRY(ensure(h, B_Y, (size_t)n * Kp, &u.Y));
   KSVD_TRY(ensure(h, B_GN2, (size_t)Kp, &u.gn2));
   KSVD_TRY(ensure(h, B_C, (size_t)Kp * Kp, &u.C));
-  KSVD_TRY(ensure(h, B_AVEC, (size_t)2 * n, &u.avec));
-  KSVD_TRY(ensure(h, B_AD, (size_t)Kp, &u.aD));
+  KSVD_TRY(ensure(h, B_AVEC, (size_t)3 * n, &u.avec));
+  KSVD_TRY(ensure(h, B_AD, (size_t)2 * Kp, &u.aD));
+  KSVD_TRY(ensure(h, B_G, (size_t)Kp * Kp, &u.G));
+  KSVD_TRY(ensure(h, B_P, (size_t)Kp * Kp, &u.P));
   KSVD_TRY(ensure(h, B_PART, (size_t)4 * (nctas + 1), &u.part));
   KSVD_TRY(ensure(h, B_UNUSED, (size_t)N, &u.unused));
   KSVD_TRY(ensure(h, B_BITMAP, (size_t)N, &u.bitmap));
@@ -247,6 +306,7 @@ ksvd_status run_update(ksvd_handle* h, float* Dp, const float* X, int64_t N, con
   UpdateArgs u;
   KSVD_TRY(update_ws(h, N, u));
   u.X = X; u.D = Dp; u.idx = idx; u.coef = coef; u.nnz = nnz; u.perm = perm_dev;
+  KSVD_TRY(gram_padded(h, Dp, u.G));          // the sweep maintains G = D'D from here on
   {
     StageScope sc(h, KSVD_STAGE_LISTS);
     KSVD_CK(h, launch_update_prepare(u, h->stream));
@@ -461,6 +521,16 @@ ksvd_status ksvd_normcols(ksvd_handle* h, float* D) {
 ksvd_status ksvd_gram(ksvd_handle* h, const float* D, float* G) {
   if (!h || bad_ptr(D) || bad_ptr(G)) return KSVD_ERR_INVALID_ARGUMENT;
   const int n = h->p.n, K = h->p.K;
+  if (mixed(h)) {
+    float *Dp = nullptr;
+    TcOperand d;
+    int* de = nullptr;
+    KSVD_TRY(ensure(h, B_DEVERR, 1, &de));
+    KSVD_TRY(load_dict(h, D, &Dp));
+    KSVD_TRY(split_dict(h, Dp, &d));
+    KSVD_CK(h, launch_gemm_tn_bf16(d, d, G, K, K, K, n, 3, de, h->stream));
+    return KSVD_OK;
+  }
   KSVD_CK(h, launch_gemm_tn_f32(D, n, D, n, G, K, K, K, K, K, n, h->stream));
   return KSVD_OK;
 }
@@ -468,6 +538,18 @@ ksvd_status ksvd_gram(ksvd_handle* h, const float* D, float* G) {
 ksvd_status ksvd_dtx(ksvd_handle* h, const float* D, const float* X, int64_t N, float* A0) {
   if (!h || bad_ptr(D) || bad_ptr(X) || bad_ptr(A0) || N < 0) return KSVD_ERR_INVALID_ARGUMENT;
   const int n = h->p.n, K = h->p.K;
+  if (mixed(h)) {
+    float* Dp = nullptr;
+    TcOperand d, x;
+    int* de = nullptr;
+    KSVD_TRY(ensure(h, B_DEVERR, 1, &de));
+    KSVD_TRY(load_dict(h, D, &Dp));
+    KSVD_TRY(split_dict(h, Dp, &d));
+    KSVD_TRY(split_signals(h, X, N, &x));
+    drop_xsplit(h);
+    KSVD_CK(h, launch_gemm_tn_bf16(d, x, A0, K, K, N, n, 3, de, h->stream));
+    return KSVD_OK;
+  }
   KSVD_CK(h, launch_gemm_tn_f32(D, n, X, n, A0, K, K, K, N, N, n, h->stream));
   return KSVD_OK;
 }
@@ -495,6 +577,7 @@ ksvd_status ksvd_omp(ksvd_handle* h, const float* D, const float* X, int64_t N, 
   if (!h || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || N < 0)
     return KSVD_ERR_INVALID_ARGUMENT;
   if (N == 0) return KSVD_OK;
+  drop_xsplit(h);
   float *Dp = nullptr, *G = nullptr, *A0 = nullptr, *xn2 = nullptr;
   KSVD_TRY(load_dict(h, D, &Dp));
   KSVD_TRY(ensure(h, B_G, (size_t)h->Kp * h->Kp, &G));
@@ -505,6 +588,7 @@ ksvd_status ksvd_omp(ksvd_handle* h, const float* D, const float* X, int64_t N, 
     KSVD_TRY(ensure(h, B_XN2, (size_t)N, &xn2));
     KSVD_CK(h, launch_col_norm2(X, h->p.n, N, xn2, h->stream));
   }
+  drop_xsplit(h);
   return run_omp(h, G, A0, N, xn2, eps2, idx, coef, nnz);
 }
 
@@ -585,6 +669,7 @@ ksvd_status ksvd_iterate(ksvd_handle* h, float* D, const float* X, int64_t N, in
   if ((int64_t)N * h->p.T > 0x7fffffffLL)
     return fail(h, KSVD_ERR_UNSUPPORTED, "N*T must stay below 2^31%s");
   const int Kp = h->Kp;
+  drop_xsplit(h);
   float *Dp = nullptr, *G = nullptr, *A0 = nullptr;
   double* rd = nullptr;
   int32_t *pd = nullptr, *cd = nullptr;
@@ -604,6 +689,7 @@ ksvd_status ksvd_iterate(ksvd_handle* h, float* D, const float* X, int64_t N, in
     KSVD_TRY(gram_padded(h, Dp, G));                                   // G of the updated D
     KSVD_TRY(run_clear(h, Dp, G, X, N, cd));                           // KSVD.cu:126
   }
+  drop_xsplit(h);
   KSVD_TRY(store_dict(h, Dp, D));
   if (rmse && iters > 0)
     KSVD_CK(h, cudaMemcpyAsync(rmse, rd, sizeof(double) * iters, cudaMemcpyDeviceToHost,

@@ -23,7 +23,10 @@ struct TcOperand {
   int64_t rows;         // rows available (multiple of the tile)
 };
 cudaError_t launch_gemm_tn_bf16(const TcOperand& A, const TcOperand& B, float* C, int64_t ldc,
-                                int M, int64_t Ncols, int inner, int passes, cudaStream_t st);
+                                int M, int64_t Ncols, int inner, int passes, int* dev_err,
+                                cudaStream_t st);
+int tc_tile_atoms();
+int tc_tile_signals();
 // hi/lo split of an FP32 matrix stored as `rows` rows of `inner` contiguous floats (ld_in),
 // written with leading dimension ld_out (zero padded to ld_out and to rows_out).
 cudaError_t launch_split_bf16(const float* in, int64_t ld_in, int64_t rows, int inner,
@@ -68,8 +71,10 @@ struct UpdateArgs {
   float* Y;              // n x Kp
   float* gn2;            // Kp
   float* C;              // Kp x Kp co-occurrence, C(i,j) = sum_s Gamma(i,s) Gamma(j,s)
-  float* avec;           // n (atom accumulator, zero between atoms)
-  float* aD;             // Kp
+  float* G;              // Kp x Kp, D'D of the current dictionary on entry, maintained
+  float* P;              // Kp x Kp, D'Y (P(i,j) = d_i . Y_j), maintained
+  float* avec;           // 3 x n rotating atom accumulators (zero on entry)
+  float* aD;             // 2 x Kp alternating a'D slices
   float* part;           // nctas x 4 scratch
   int32_t* unused;       // N
   int32_t* bitmap;       // N

@@ -38,7 +38,7 @@ __device__ __forceinline__ void put(V (&a)[SPL], int j, V v) {
 }
 
 template <int KPL, int TMAX>
-__global__ void __launch_bounds__(kOmpWarps * 32, 2)
+__global__ void __launch_bounds__(kOmpWarps * 32, (TMAX <= 32 ? 3 : 1))
 omp_kernel(const float* __restrict__ G, int64_t ldg, const float* __restrict__ A0, int64_t lda,
            int K, int64_t N, int T, const float* __restrict__ xnorm2,
            const float* __restrict__ eps2, int32_t* __restrict__ idx_out,
@@ -46,23 +46,25 @@ omp_kernel(const float* __restrict__ G, int64_t ldg, const float* __restrict__ A
   constexpr int M4 = KPL / 4;    // float4 groups per lane; lane owns rows 128*m + 4*lane + q
   constexpr int SPL = TMAX / 32; // support slots per lane; lane owns slots lane + 32*j
   constexpr int LS = TMAX + 1;   // row stride of L in shared memory
-  extern __shared__ float smem[];
+  extern __shared__ __align__(16) float smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  float* L = smem + (size_t)wib * TMAX * LS;
+  float* L = smem + (size_t)wib * (TMAX * LS + 32 * KPL);   // Cholesky factor, (TMAX x LS)
+  float* a0s = L + TMAX * LS;                                // this warp's alpha0 column
   const int64_t warps_total = (int64_t)gridDim.x * kOmpWarps;
   bool numeric_bad = false;
 
   for (int64_t s = (int64_t)blockIdx.x * kOmpWarps + wib; s < N; s += warps_total) {
-    float a0[M4][4], al[M4][4];
+    float al[M4][4];
     const float* a0p = A0 + s * lda + 4 * lane;
+    __syncwarp();                      // the previous signal's last reads of a0s are done
 #pragma unroll
     for (int m = 0; m < M4; ++m) {
-      float4 v = __ldcs(reinterpret_cast<const float4*>(a0p + 128 * m));
-      a0[m][0] = v.x; a0[m][1] = v.y; a0[m][2] = v.z; a0[m][3] = v.w;
-#pragma unroll
-      for (int q = 0; q < 4; ++q) al[m][q] = a0[m][q];
+      const float4 v = __ldcs(reinterpret_cast<const float4*>(a0p + 128 * m));
+      *reinterpret_cast<float4*>(a0s + 128 * m + 4 * lane) = v;
+      al[m][0] = v.x; al[m][1] = v.y; al[m][2] = v.z; al[m][3] = v.w;
     }
+    __syncwarp();
     int ind[SPL];
     float y[SPL], c[SPL];
 #pragma unroll
@@ -75,8 +77,8 @@ omp_kernel(const float* __restrict__ G, int64_t ldg, const float* __restrict__ A
     int i = 0;
     while (i < T) {
       if (emode && r2 <= e2) break;
-      // ---- argmax |alpha| (first maximum) with alpha_p and alpha0_p as payload
-      float bv = -1.f, bal = 0.f, ba0 = 0.f;
+      // ---- argmax |alpha| (first maximum) with alpha_p as payload
+      float bv = -1.f, bal = 0.f;
       int bk = 0x7fffffff;
 #pragma unroll
       for (int m = 0; m < M4; ++m)
@@ -84,18 +86,18 @@ omp_kernel(const float* __restrict__ G, int64_t ldg, const float* __restrict__ A
         for (int q = 0; q < 4; ++q) {
           const int k = 128 * m + 4 * lane + q;
           const float v = al[m][q] * al[m][q];
-          if (k < K && v > bv) { bv = v; bk = k; bal = al[m][q]; ba0 = a0[m][q]; }
+          if (k < K && v > bv) { bv = v; bk = k; bal = al[m][q]; }
         }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         const float ov = __shfl_xor_sync(KSVD_FULL_MASK, bv, o);
         const int ok = __shfl_xor_sync(KSVD_FULL_MASK, bk, o);
         const float oal = __shfl_xor_sync(KSVD_FULL_MASK, bal, o);
-        const float oa0 = __shfl_xor_sync(KSVD_FULL_MASK, ba0, o);
-        if (ov > bv || (ov == bv && ok < bk)) { bv = ov; bk = ok; bal = oal; ba0 = oa0; }
+        if (ov > bv || (ov == bv && ok < bk)) { bv = ov; bk = ok; bal = oal; }
       }
       if (bk >= K) { numeric_bad = true; break; }   // every |alpha| was NaN
       const int p = bk;
+      const float ba0 = a0s[p];
       bool dup = false;
 #pragma unroll
       for (int j = 0; j < SPL; ++j) dup |= (lane + 32 * j < i) && ind[j] == p;
@@ -189,9 +191,13 @@ omp_kernel(const float* __restrict__ G, int64_t ldg, const float* __restrict__ A
           }
         }
 #pragma unroll
-        for (int m = 0; m < M4; ++m)
-#pragma unroll
-          for (int q = 0; q < 4; ++q) al[m][q] = a0[m][q] - al[m][q];
+        for (int m = 0; m < M4; ++m) {
+          const float4 a = *reinterpret_cast<const float4*>(a0s + 128 * m + 4 * lane);
+          al[m][0] = a.x - al[m][0];
+          al[m][1] = a.y - al[m][1];
+          al[m][2] = a.z - al[m][2];
+          al[m][3] = a.w - al[m][3];
+        }
       }
     }
     // ---- outputs: slots in selection order, -1 / 0 padding
@@ -214,7 +220,7 @@ template <int KPL, int TMAX>
 cudaError_t launch_omp_t(const float* G, int64_t ldg, const float* A0, int64_t lda, int K,
                          int64_t N, int T, const float* xnorm2, const float* eps2, int32_t* idx,
                          float* coef, int32_t* nnz, int* dev_err, cudaStream_t st) {
-  const size_t smem = (size_t)kOmpWarps * TMAX * (TMAX + 1) * sizeof(float);
+  const size_t smem = (size_t)kOmpWarps * (TMAX * (TMAX + 1) + 32 * KPL) * sizeof(float);
   auto kern = omp_kernel<KPL, TMAX>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);

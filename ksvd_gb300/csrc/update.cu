@@ -149,8 +149,11 @@ __global__ void list_fill_kernel(const int32_t* __restrict__ idx, const int32_t*
 
 // ---- 2. per-atom precompute -------------------------------------------------------------------
 
-// CTA j: gn2[j], Y(:,j), C(:,j) from the atom's list.  Each warp walks every 8th entry and keeps
-// private partials (deterministic), reduced in warp order at the end.
+// CTA j: gn2[j], Y(:,j), C(:,j) from the atom's list.  Each warp walks every 8th entry, two
+// entries in flight, with its share of Y_j in registers (NPL rows per lane) and its share of
+// C(:,j) in a private shared-memory vector; the warp partials are summed in warp order at the
+// end, so the result is deterministic.
+template <int NPL>
 __global__ void __launch_bounds__(kPrepThreads)
 prepare_kernel(const float* __restrict__ X, int n, int T, int Kp, const int32_t* __restrict__ idx,
                const float* __restrict__ coef, const int32_t* __restrict__ nnz,
@@ -164,45 +167,78 @@ prepare_kernel(const float* __restrict__ X, int n, int T, int Kp, const int32_t*
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int j = blockIdx.x;
   for (int i = threadIdx.x; i < NW * Kp; i += blockDim.x) Cw[i] = 0.f;
-  for (int i = threadIdx.x; i < NW * n; i += blockDim.x) Yw[i] = 0.f;
   __syncthreads();
   const int64_t q0 = start[j], q1 = start[j + 1];
   float* cw = Cw + (size_t)w * Kp;
-  float* yw = Yw + (size_t)w * n;
+  float acc[NPL];
+#pragma unroll
+  for (int i = 0; i < NPL; ++i) acc[i] = 0.f;
   float g2 = 0.f;
-  for (int64_t q = q0 + w; q < q1; q += NW) {
-    const int64_t e = list[q];
-    const int64_t s = e / T;
-    const float g = coef[e];
-    g2 = fmaf(g, g, g2);
-    const float* x = X + s * n;
-    for (int r = lane; r < n; r += 32) yw[r] = fmaf(g, x[r], yw[r]);
+  auto scatter = [&](int64_t s, float g) {
     const int nz = min(nnz[s], T);
     for (int t = lane; t < nz; t += 32) {
       const int i = idx[s * T + t];
       if (i >= 0 && i < Kp) cw[i] = fmaf(g, coef[s * T + t], cw[i]);   // distinct per signal
     }
     __syncwarp();
+  };
+  int64_t q = q0 + w;
+  for (; q + NW < q1; q += 2 * NW) {
+    const int64_t e0 = list[q], e1 = list[q + NW];
+    const int64_t s0 = e0 / T, s1 = e1 / T;
+    const float ga = coef[e0], gb = coef[e1];
+    const float* xa = X + s0 * n;
+    const float* xb = X + s1 * n;
+    float va[NPL], vb[NPL];
+#pragma unroll
+    for (int i = 0; i < NPL; ++i) {
+      const int r = lane + 32 * i;
+      va[i] = r < n ? __ldg(xa + r) : 0.f;
+      vb[i] = r < n ? __ldg(xb + r) : 0.f;
+    }
+#pragma unroll
+    for (int i = 0; i < NPL; ++i) acc[i] = fmaf(gb, vb[i], fmaf(ga, va[i], acc[i]));
+    g2 = fmaf(gb, gb, fmaf(ga, ga, g2));
+    scatter(s0, ga);
+    scatter(s1, gb);
+  }
+  if (q < q1) {
+    const int64_t e0 = list[q];
+    const int64_t s0 = e0 / T;
+    const float ga = coef[e0];
+    const float* xa = X + s0 * n;
+#pragma unroll
+    for (int i = 0; i < NPL; ++i) {
+      const int r = lane + 32 * i;
+      if (r < n) acc[i] = fmaf(ga, __ldg(xa + r), acc[i]);
+    }
+    g2 = fmaf(ga, ga, g2);
+    scatter(s0, ga);
+  }
+#pragma unroll
+  for (int i = 0; i < NPL; ++i) {
+    const int r = lane + 32 * i;
+    if (r < n) Yw[(size_t)w * n + r] = acc[i];
   }
   if (lane == 0) g2w[w] = g2;
   __syncthreads();
   for (int i = threadIdx.x; i < Kp; i += blockDim.x) {
-    float acc = 0.f;
+    float a = 0.f;
 #pragma unroll
-    for (int ww = 0; ww < NW; ++ww) acc += Cw[(size_t)ww * Kp + i];
-    C[(int64_t)j * Kp + i] = acc;
+    for (int ww = 0; ww < NW; ++ww) a += Cw[(size_t)ww * Kp + i];
+    C[(int64_t)j * Kp + i] = a;
   }
   for (int r = threadIdx.x; r < n; r += blockDim.x) {
-    float acc = 0.f;
+    float a = 0.f;
 #pragma unroll
-    for (int ww = 0; ww < NW; ++ww) acc += Yw[(size_t)ww * n + r];
-    Y[(int64_t)j * n + r] = acc;
+    for (int ww = 0; ww < NW; ++ww) a += Yw[(size_t)ww * n + r];
+    Y[(int64_t)j * n + r] = a;
   }
   if (threadIdx.x == 0) {
-    float acc = 0.f;
+    float a = 0.f;
 #pragma unroll
-    for (int ww = 0; ww < NW; ++ww) acc += g2w[ww];
-    gn2[j] = acc;
+    for (int ww = 0; ww < NW; ++ww) a += g2w[ww];
+    gn2[j] = a;
   }
 }
 
@@ -214,11 +250,20 @@ __global__ void init_state_kernel(int64_t N, int Kp, int32_t* __restrict__ unuse
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t s = t; s < N; s += stride) { unused[s] = (int32_t)s; bitmap[s] = 1; }
   for (int64_t k = t; k < Kp; k += stride) { replaced[k] = 0; usecount[k] = 0; }
-  for (int64_t r = t; r < 2 * n; r += stride) avec[r] = 0.f;
+  for (int64_t r = t; r < 3 * n; r += stride) avec[r] = 0.f;
   if (t == 0) { *counter = 0; barrier[0] = 0; barrier[1] = 0; }
 }
 
 // ---- 3. the sweep -------------------------------------------------------------------------------
+//
+// Pipelined schedule: one grid barrier per atom.  With j the current atom and j' the next one:
+//   a(j') = Y_j' - sum_k v_k d_k + ||gamma_j'||^2 d_j',  v = C(:, j'), v_j' = ||gamma_j'||^2
+//   a(j')'D = P(:, j') - G v + ||gamma_j'||^2 G(:, j')        (G = D'D, P = D'Y, both maintained)
+// While atom j's coefficients are being recomputed, every CTA already accumulates its slice of
+// a'(j') and a'(j')'D with the k = j term left out (d_j, C(j, j'), G(:, j), P(j, :) are being
+// rewritten in that same phase).  After the barrier every CTA folds the missing term back in
+// with the scalar c = C(j, j'):  a(j') = a'(j') - c d_j,  a(j')'d_i = a'(j')'d_i - c G(i, j)
+// (i != j) and a(j')'d_j directly.  Rows of C, G, P that a phase rewrites are never read in it.
 
 __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
   unsigned v;
@@ -226,14 +271,18 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
   return v;
 }
 
-// Sense-free generation barrier over all CTAs of a cooperative launch.  Bounded: returns false
-// (and records kDevErrTimeout) if the generation does not advance within the spin limit.
+__device__ __forceinline__ void prefetch_l2_bulk(const void* p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// Generation barrier over all CTAs of the cooperative launch.  Bounded: returns false (and
+// records kDevErrTimeout) if the generation does not advance within the spin limit.
 __device__ bool grid_barrier(unsigned* bar, unsigned nctas, int* dev_err, int* sflag) {
-  __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
     const unsigned gen = ld_acquire_gpu(bar + 1);
+    __threadfence();
     const unsigned arrived = atomicAdd(bar, 1u) + 1u;
     if (arrived == nctas) {
       atomicExch(bar, 0u);
@@ -243,10 +292,9 @@ __device__ bool grid_barrier(unsigned* bar, unsigned nctas, int* dev_err, int* s
       unsigned spins = 0;
       while (ld_acquire_gpu(bar + 1) == gen) {
         if (++spins > kBarrierSpinLimit) { ok = 0; atomicOr(dev_err, kDevErrTimeout); break; }
-        __nanosleep(64);
+        if (spins > 4096) __nanosleep(100);
       }
     }
-    __threadfence();
     *sflag = ok;
   }
   __syncthreads();
@@ -270,8 +318,10 @@ struct SweepArgs {
   const float* Y;
   const float* gn2;
   float* C;
-  float* avec;
-  float* aD;
+  float* G;
+  float* P;
+  float* avec;     // 3 x n
+  float* aDbuf;    // 2 x Kp
   float* part;
   int32_t* unused;
   int32_t* bitmap;
@@ -282,177 +332,355 @@ struct SweepArgs {
   int* dev_err;
 };
 
-__global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
-  constexpr int NW = kSweepThreads / 32;
-  extern __shared__ float sm[];
-  float* a_s = sm;                    // n
-  float* aD_s = sm + A.n;             // Kp
-  float* cpart = aD_s + A.Kp;         // Kp
-  __shared__ float red_f[64];
-  __shared__ int red_i[64];
-  __shared__ int sflag;
-  __shared__ int use_cnt;
-  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-  const int c = blockIdx.x, nctas = gridDim.x;
-  const int n = A.n, K = A.K, Kp = A.Kp, T = A.T;
-  // atom slice of this CTA (for P1 / P2 / zeroing)
-  const int kper = (K + nctas - 1) / nctas;
-  const int k0 = min(K, c * kper), k1 = min(K, k0 + kper);
+template <int NPL>
+struct Sweep {
+  static constexpr int NW = kSweepThreads / 32;
+  static constexpr int EB = NPL <= 8 ? 4 : (NPL <= 16 ? 2 : 1);   // entries per warp batch
+  const SweepArgs& A;
+  float* a_s;      // n     current atom vector a(j)
+  float* aD_s;     // Kp    a(j)'D
+  float* cpart;    // Kp    this CTA's part of the new row j of C
+  float* v_s;      // Kp    C(:, j') for the next atom
+  float* red_f;
+  int* red_i;
+  int* sflag;
+  int tid, lane, w, c, nctas, k0, k1;
 
-  for (int jj = 0; jj < K; ++jj) {
-    const int j = A.perm[jj];
-    if (j < 0 || j >= K) {                       // not a permutation entry: skip the atom
-      if (c == 0 && tid == 0) atomicOr(A.dev_err, kDevErrBounds);
-      continue;
-    }
-    const int64_t q0 = A.start[j], q1 = A.start[j + 1];
-    const int64_t cnt = q1 - q0;
-    if (cnt == 0) {
-      // ---- special case: replace the unused atom by the worst-represented unused signal
-      const int64_t counter = *((volatile int64_t*)A.counter);
-      const int64_t ncand = min((int64_t)A.max_signals, A.N - counter);
-      if (ncand <= 0) continue;
-      float best_v = -1.f;
-      int best_b = 0x7fffffff;
-      for (int64_t b = (int64_t)c * NW + w; b < ncand; b += (int64_t)nctas * NW) {
-        const int64_t s = __ldcg(A.unused + b);
-        const float* x = A.X + s * n;
-        const int nz = min(A.nnz[s], T);
-        float e = 0.f;
-        for (int r = lane; r < n; r += 32) {
-          float v = x[r];
-          for (int t = 0; t < nz; ++t) {
-            const int i = A.idx[s * T + t];
-            if (i >= 0 && i < K)
-              v = fmaf(-__ldcg(A.coef + s * T + t), __ldcg(A.D + (int64_t)i * n + r), v);
-          }
-          e = fmaf(v, v, e);
-        }
-        e = warp_sum(e);
-        if (e > best_v) { best_v = e; best_b = (int)b; }
-      }
-      block_argmax(best_v, best_b, red_f, red_i);
-      if (tid == 0) {
-        A.part[c * 4 + 0] = best_v;
-        reinterpret_cast<int*>(A.part)[c * 4 + 1] = best_b;
-      }
-      if (!grid_barrier(A.barrier, nctas, A.dev_err, &sflag)) return;
-      if (c == 0) {
-        float v = -1.f;
-        int bi = 0x7fffffff;
-        for (int cc = lane; cc < nctas; cc += 32) {
-          const float pv = ((volatile float*)A.part)[cc * 4 + 0];
-          const int pb = ((volatile int*)A.part)[cc * 4 + 1];
-          if (pv > v || (pv == v && pb < bi)) { v = pv; bi = pb; }
-        }
-        if (w == 0) warp_argmax(v, bi);
-        if (w == 0 && lane == 0) red_i[0] = bi;
-        __syncthreads();
-        const int bsel = red_i[0];
-        if (bsel >= 0 && bsel < ncand) {
-          const int64_t s = __ldcg(A.unused + bsel);
-          const float* x = A.X + s * n;
-          float nr = 0.f;
-          for (int r = tid; r < n; r += blockDim.x) nr = fmaf(x[r], x[r], nr);
-          nr = sqrtf(block_sum(nr, red_f));
-          for (int r = tid; r < n; r += blockDim.x) A.D[(int64_t)j * n + r] = x[r] / nr;
-          if (tid == 0) {
-            A.unused[bsel] = __ldcg(A.unused + (A.N - counter - 1));
-            *A.counter = counter + 1;
-            A.replaced[j] = 1;
-            A.bitmap[s] = 0;
-          }
-        } else if (tid == 0) {
-          atomicOr(A.dev_err, kDevErrBounds);
-        }
-      }
-      if (!grid_barrier(A.barrier, nctas, A.dev_err, &sflag)) return;
-      continue;
-    }
+  __device__ Sweep(const SweepArgs& a, float* sm, float* rf, int* ri, int* sf)
+      : A(a), red_f(rf), red_i(ri), sflag(sf) {
+    a_s = sm;
+    aD_s = a_s + A.n;
+    cpart = aD_s + A.Kp;
+    v_s = cpart + A.Kp;
+    tid = threadIdx.x;
+    lane = tid & 31;
+    w = tid >> 5;
+    c = blockIdx.x;
+    nctas = gridDim.x;
+    const int kper = (A.K + nctas - 1) / nctas;
+    k0 = min(A.K, c * kper);
+    k1 = min(A.K, k0 + kper);
+  }
 
-    // ---- P1: a += slice of (-D v), CTA 0 adds Y_j + d_j ||gamma_j||^2; zero C row j slice.
-    // The accumulator avec is zero here: it starts zeroed and P3 clears it after use.
-    float* acc_vec = A.avec;
-    const float g2j = A.gn2[j];
-    for (int r = tid; r < n; r += blockDim.x) {
-      float acc = 0.f;
-      for (int k = k0; k < k1; ++k) {
-        const float vk = (k == j) ? g2j : __ldcg(A.C + (int64_t)j * Kp + k);
-        acc = fmaf(-vk, __ldcg(A.D + (int64_t)k * n + r), acc);
-      }
-      if (c == 0)
-        acc += A.Y[(int64_t)j * n + r] + __ldcg(A.D + (int64_t)j * n + r) * g2j;
-      if (k1 > k0 || c == 0) atomicAdd(acc_vec + r, acc);
-    }
-    for (int k = k0 + tid; k < k1; k += blockDim.x) A.C[(int64_t)k * Kp + j] = 0.f;
-    if (!grid_barrier(A.barrier, nctas, A.dev_err, &sflag)) return;
+  __device__ bool barrier() { return grid_barrier(A.barrier, nctas, A.dev_err, sflag); }
 
-    // ---- P2: a to shared memory, ||a||, a'D for this CTA's atom slice
-    for (int r = tid; r < n; r += blockDim.x) a_s[r] = __ldcg(acc_vec + r);
+  // Slices of a'(jn) and a'(jn)'D leaving out atom jx (jx = -1: nothing left out).
+  __device__ void next_partials(int jn, int jx, float* avec_slot, float* aD_slot) {
+    const int n = A.n, K = A.K, Kp = A.Kp;
+    const float g2 = A.gn2[jn];
+    for (int k = tid; k < Kp; k += blockDim.x)
+      v_s[k] = (k >= K || k == jx) ? 0.f : (k == jn ? g2 : __ldcg(A.C + (int64_t)jn * Kp + k));
     __syncthreads();
-    for (int k = k0 + w; k < k1; k += NW) {
-      const float* d = A.D + (int64_t)k * n;
-      float acc = 0.f;
-      for (int r = lane; r < n; r += 32) acc = fmaf(__ldcg(d + r), a_s[r], acc);
-      acc = warp_sum(acc);
-      if (lane == 0) A.aD[k] = acc;
-    }
-    if (!grid_barrier(A.barrier, nctas, A.dev_err, &sflag)) return;
-
-    // ---- P3: new coefficients of atom j, new d_j, refreshed C row j, use count of atom j
-    float nr = 0.f;
-    for (int r = tid; r < n; r += blockDim.x) nr = fmaf(a_s[r], a_s[r], nr);
-    const float anorm = sqrtf(block_sum(nr, red_f));
-    for (int k = tid; k < Kp; k += blockDim.x) {
-      aD_s[k] = k < K ? __ldcg(A.aD + k) : 0.f;
-      cpart[k] = 0.f;
-    }
-    if (tid == 0) use_cnt = 0;
-    __syncthreads();
-    if (c == 0)
+    if (k1 > k0 || c == 0) {
       for (int r = tid; r < n; r += blockDim.x) {
-        A.D[(int64_t)j * n + r] = a_s[r] / anorm;
-        acc_vec[r] = 0.f;   // every CTA has read the accumulator (P2, before the barrier)
+        float acc = 0.f;
+#pragma unroll 4
+        for (int k = k0; k < k1; ++k)
+          if (k != jx) acc = fmaf(-v_s[k], __ldcg(A.D + (int64_t)k * n + r), acc);
+        if (c == 0) acc += A.Y[(int64_t)jn * n + r] + g2 * __ldcg(A.D + (int64_t)jn * n + r);
+        atomicAdd(avec_slot + r, acc);
       }
+    }
+    for (int i = k0 + w; i < k1; i += NW) {
+      if (i == jx) continue;
+      const float* gi = A.G + (int64_t)i * Kp;       // column i of G = row i
+      float acc = 0.f;
+      for (int k = lane; k < K; k += 32)
+        if (k != jx) acc = fmaf(__ldcg(gi + k), v_s[k], acc);
+      acc = warp_sum(acc);
+      if (lane == 0)
+        aD_slot[i] = __ldcg(A.P + (int64_t)jn * Kp + i) - acc +
+                     g2 * __ldcg(A.G + (int64_t)jn * Kp + i);
+    }
+  }
+
+  // Row jn of C is rebuilt by atom jn's phase: clear this CTA's slice of it.
+  __device__ void zero_row(int jn) {
+    for (int k = k0 + tid; k < k1; k += blockDim.x) A.C[(int64_t)k * A.Kp + jn] = 0.f;
+  }
+
+  // Atom j's new column d_j is in D: G(:, j), G(j, :), P(j, :) for this CTA's slice.
+  // scale = 1/||a|| when a_s holds the unnormalised atom (regular path) -- then G comes from
+  // aD_s -- or 0 when a_s already holds d_j (special case) and G is recomputed from D.
+  __device__ void refresh_gp(int j, float inv_norm, bool from_aD) {
+    const int n = A.n, Kp = A.Kp;
+    for (int i = k0 + w; i < k1; i += NW) {
+      float g, pj;
+      const float* yi = A.Y + (int64_t)i * n;
+      float accp = 0.f, accg = 0.f;
+      for (int r = lane; r < n; r += 32) {
+        accp = fmaf(a_s[r], __ldg(yi + r), accp);
+        if (!from_aD) accg = fmaf(a_s[r], __ldcg(A.D + (int64_t)i * n + r), accg);
+      }
+      accp = warp_sum(accp);
+      if (!from_aD) accg = warp_sum(accg);
+      pj = accp * inv_norm;
+      g = from_aD ? aD_s[i] * inv_norm : accg * inv_norm;
+      if (i == j) g = 1.f;
+      if (lane == 0) {
+        A.G[(int64_t)j * Kp + i] = g;
+        A.G[(int64_t)i * Kp + j] = g;
+        A.P[(int64_t)i * Kp + j] = pj;
+      }
+    }
+  }
+
+  // Fold the left-out atom prev back into a(j) and a(j)'D; returns ||a(j)||.
+  __device__ float correct(int j, int prev, const float* avec_slot, const float* aD_slot) {
+    const int n = A.n, K = A.K, Kp = A.Kp;
+    const float cp = prev >= 0 ? __ldcg(A.C + (int64_t)j * Kp + prev) : 0.f;
+    for (int r = tid; r < n; r += blockDim.x) {
+      float v = __ldcg(avec_slot + r);
+      if (prev >= 0) v = fmaf(-cp, __ldcg(A.D + (int64_t)prev * n + r), v);
+      a_s[r] = v;
+    }
+    __syncthreads();
+    for (int i = tid; i < Kp; i += blockDim.x) {
+      float v = 0.f;
+      if (i < K && i != prev) {
+        v = __ldcg(aD_slot + i);
+        if (prev >= 0) v = fmaf(-cp, __ldcg(A.G + (int64_t)prev * Kp + i), v);
+      }
+      aD_s[i] = v;
+      cpart[i] = 0.f;
+    }
+    float dp = 0.f, nn = 0.f;
+    for (int r = tid; r < n; r += blockDim.x) {
+      nn = fmaf(a_s[r], a_s[r], nn);
+      if (prev >= 0) dp = fmaf(__ldcg(A.D + (int64_t)prev * n + r), a_s[r], dp);
+    }
+    nn = block_sum(nn, red_f);
+    if (prev >= 0) {
+      dp = block_sum(dp, red_f);
+      if (tid == 0) aD_s[prev] = dp;
+    }
+    __syncthreads();
+    return sqrtf(nn);
+  }
+
+  // Issue L2 prefetches of the signals (and their codes) the next atom will read.
+  __device__ void prefetch_next(int jn) {
+    const int64_t q0 = A.start[jn], cnt = A.start[jn + 1] - q0;
+    const int64_t per = (cnt + nctas - 1) / nctas;
+    const int64_t qa = q0 + min(cnt, (int64_t)c * per), qb = q0 + min(cnt, (int64_t)(c + 1) * per);
+    const bool bulk_x = (A.n & 3) == 0, bulk_c = (A.T & 3) == 0;
+    for (int64_t q = qa + tid; q < qb; q += blockDim.x) {
+      const int64_t s = A.list[q] / A.T;
+      const float* x = A.X + s * A.n;
+      if (bulk_x) prefetch_l2_bulk(x, (uint32_t)A.n * 4);
+      if (bulk_c) {
+        prefetch_l2_bulk(A.coef + s * A.T, (uint32_t)A.T * 4);
+        prefetch_l2_bulk(A.idx + s * A.T, (uint32_t)A.T * 4);
+      }
+    }
+  }
+
+  // New coefficients of atom j for this CTA's share of its signals; C row j and use count.
+  __device__ void update_coefs(int j, int64_t q0, int64_t cnt, float anorm, int* use_cnt) {
+    const int n = A.n, K = A.K, T = A.T;
     const float aDj = aD_s[j];
     const int64_t per = (cnt + nctas - 1) / nctas;
     const int64_t qa = q0 + min(cnt, (int64_t)c * per), qb = q0 + min(cnt, (int64_t)(c + 1) * per);
     int my_use = 0;
-    for (int64_t q = qa + w; q < qb; q += NW) {
-      const int64_t e = A.list[q];
-      const int64_t s = e / T;
-      const float* x = A.X + s * n;
-      float ax = 0.f;
-#pragma unroll 4
-      for (int r = lane; r < n; r += 32) ax = fmaf(a_s[r], __ldcs(x + r), ax);
-      const int nz = min(A.nnz[s], T);
-      float gs = 0.f;
-      for (int t = lane; t < nz; t += 32) {
-        const int i = A.idx[s * T + t];
-        if (i >= 0 && i < K) gs = fmaf(__ldcg(A.coef + s * T + t), aD_s[i], gs);
+    for (int64_t qs = qa + (int64_t)w * EB; qs < qb; qs += (int64_t)NW * EB) {
+      const int ne = (int)min((int64_t)EB, qb - qs);
+      int64_t e[EB], s[EB];
+      int nz[EB];
+#pragma unroll
+      for (int b = 0; b < EB; ++b) {
+        e[b] = b < ne ? A.list[qs + b] : 0;
+        s[b] = e[b] / T;
+        nz[b] = b < ne ? min(A.nnz[s[b]], T) : 0;
       }
-      ax = warp_sum(ax);
-      gs = warp_sum(gs);
-      const float gold = __ldcg(A.coef + e);
-      const float g = (ax - gs + aDj * gold) / anorm;
-      for (int t = lane; t < nz; t += 32) {
-        const int i = A.idx[s * T + t];
-        if (i != j && i >= 0 && i < K) atomicAdd(cpart + i, g * __ldcg(A.coef + s * T + t));
+      float xv[EB][NPL];
+#pragma unroll
+      for (int b = 0; b < EB; ++b)
+#pragma unroll
+        for (int i = 0; i < NPL; ++i) {
+          const int r = lane + 32 * i;
+          xv[b][i] = (b < ne && r < n) ? __ldcg(A.X + s[b] * n + r) : 0.f;
+        }
+      float cf[EB][2];
+      int ix[EB][2];
+#pragma unroll
+      for (int b = 0; b < EB; ++b)
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const int t = lane + 32 * u;
+          const bool ok = t < nz[b];
+          const int v = ok ? A.idx[s[b] * T + t] : -1;
+          ix[b][u] = (v >= 0 && v < K) ? v : -1;
+          cf[b][u] = ok ? __ldcg(A.coef + s[b] * T + t) : 0.f;
+        }
+      float ax[EB], gs[EB];
+#pragma unroll
+      for (int b = 0; b < EB; ++b) {
+        float acc = 0.f;
+#pragma unroll
+        for (int i = 0; i < NPL; ++i) {
+          const int r = lane + 32 * i;
+          if (r < n) acc = fmaf(a_s[r], xv[b][i], acc);
+        }
+        ax[b] = acc;
+        float g = 0.f;
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+          if (ix[b][u] >= 0) g = fmaf(cf[b][u], aD_s[ix[b][u]], g);
+        gs[b] = g;
       }
-      __syncwarp();
-      if (lane == 0) {
-        A.coef[e] = g;
-        if (g * g > 1e-7f) ++my_use;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int b = 0; b < EB; ++b) {
+          ax[b] += __shfl_xor_sync(KSVD_FULL_MASK, ax[b], o);
+          gs[b] += __shfl_xor_sync(KSVD_FULL_MASK, gs[b], o);
+        }
+#pragma unroll
+      for (int b = 0; b < EB; ++b) {
+        if (b >= ne) continue;
+        const float gold = __ldcg(A.coef + e[b]);
+        const float g = (ax[b] - gs[b] + aDj * gold) / anorm;
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+          if (ix[b][u] >= 0 && ix[b][u] != j) atomicAdd(cpart + ix[b][u], g * cf[b][u]);
+        if (lane == 0) {
+          A.coef[e[b]] = g;
+          if (g * g > 1e-7f) ++my_use;
+        }
       }
     }
-    if (lane == 0 && my_use) atomicAdd(&use_cnt, my_use);
+    if (lane == 0 && my_use) atomicAdd(use_cnt, my_use);
     __syncthreads();
     for (int k = tid; k < K; k += blockDim.x) {
       const float v = cpart[k];
-      if (v != 0.f) atomicAdd(A.C + (int64_t)k * Kp + j, v);
+      if (k != j && v != 0.f) atomicAdd(A.C + (int64_t)k * A.Kp + j, v);
     }
-    if (tid == 0 && use_cnt) atomicAdd(A.usecount + j, use_cnt);
-    if (!grid_barrier(A.barrier, nctas, A.dev_err, &sflag)) return;
+    if (tid == 0 && *use_cnt) atomicAdd(A.usecount + j, *use_cnt);
+  }
+
+  // The worst-represented of the first min(max_signals, N - counter) unused signals replaces
+  // atom j (which no signal uses).  Leaves d_j in a_s.  Two grid barriers.
+  __device__ bool special_case(int j) {
+    const int n = A.n, T = A.T, K = A.K;
+    const int64_t counter = *((volatile int64_t*)A.counter);
+    const int64_t ncand = min((int64_t)A.max_signals, A.N - counter);
+    float best_v = -1.f;
+    int best_b = 0x7fffffff;
+    for (int64_t b = (int64_t)c * NW + w; b < ncand; b += (int64_t)nctas * NW) {
+      const int64_t s = __ldcg(A.unused + b);
+      const float* x = A.X + s * n;
+      const int nz = min(A.nnz[s], T);
+      float e = 0.f;
+      for (int r = lane; r < n; r += 32) {
+        float v = x[r];
+        for (int t = 0; t < nz; ++t) {
+          const int i = A.idx[s * T + t];
+          if (i >= 0 && i < K)
+            v = fmaf(-__ldcg(A.coef + s * T + t), __ldcg(A.D + (int64_t)i * n + r), v);
+        }
+        e = fmaf(v, v, e);
+      }
+      e = warp_sum(e);
+      if (e > best_v) { best_v = e; best_b = (int)b; }
+    }
+    block_argmax(best_v, best_b, red_f, red_i);
+    if (tid == 0) {
+      A.part[c * 4 + 0] = best_v;
+      reinterpret_cast<int*>(A.part)[c * 4 + 1] = best_b;
+    }
+    if (!barrier()) return false;
+    // every CTA reduces the partials the same way (first maximum) and reads the same signal
+    float v = -1.f;
+    int bi = 0x7fffffff;
+    for (int cc = lane; cc < nctas; cc += 32) {
+      const float pv = __ldcg(A.part + cc * 4);
+      const int pb = __ldcg(reinterpret_cast<const int*>(A.part) + cc * 4 + 1);
+      if (pv > v || (pv == v && pb < bi)) { v = pv; bi = pb; }
+    }
+    warp_argmax(v, bi);
+    const bool have = ncand > 0 && bi >= 0 && bi < ncand;
+    int64_t s = 0;
+    if (have) s = __ldcg(A.unused + bi);
+    float nr = 0.f;
+    for (int r = tid; r < n; r += blockDim.x) {
+      const float x = have ? A.X[s * n + r] : __ldcg(A.D + (int64_t)j * n + r);
+      a_s[r] = x;
+      nr = fmaf(x, x, nr);
+    }
+    nr = sqrtf(block_sum(nr, red_f));
+    for (int r = tid; r < n; r += blockDim.x) a_s[r] = have ? a_s[r] / nr : a_s[r];
+    __syncthreads();
+    if (!barrier()) return false;       // every CTA has read the unused list entry
+    if (c == 0 && have) {
+      for (int r = tid; r < n; r += blockDim.x) A.D[(int64_t)j * n + r] = a_s[r];
+      if (tid == 0) {
+        A.unused[bi] = __ldcg(A.unused + (A.N - counter - 1));
+        *A.counter = counter + 1;
+        A.replaced[j] = 1;
+        A.bitmap[s] = 0;
+      }
+    }
+    return true;
+  }
+};
+
+template <int NPL>
+__global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
+  extern __shared__ float sm[];
+  __shared__ float red_f[64];
+  __shared__ int red_i[64];
+  __shared__ int sflag;
+  __shared__ int use_cnt;
+  Sweep<NPL> S(A, sm, red_f, red_i, &sflag);
+  const int K = A.K, n = A.n;
+  // every CTA checks the whole permutation itself, so all of them leave together or none does
+  int bad = 0;
+  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    const int j = A.perm[k];
+    bad |= (j < 0 || j >= K);
+  }
+  if (__syncthreads_or(bad)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(A.dev_err, kDevErrBounds);
+    return;
+  }
+  // prologue: a(perm[0]) and a(perm[0])'D in full
+  {
+    const int j0 = A.perm[0];
+    S.zero_row(j0);
+    S.next_partials(j0, -1, A.avec, A.aDbuf);
+    if (A.start[j0 + 1] > A.start[j0]) S.prefetch_next(j0);
+    if (!S.barrier()) return;
+  }
+  for (int jj = 0; jj < K; ++jj) {
+    const int j = A.perm[jj];
+    const int prev = jj > 0 ? A.perm[jj - 1] : -1;
+    const int jn = jj + 1 < K ? A.perm[jj + 1] : -1;
+    float* av_cur = A.avec + (jj % 3) * n;
+    float* av_next = A.avec + ((jj + 1) % 3) * n;
+    float* av_clear = A.avec + ((jj + 2) % 3) * n;
+    const float* ad_cur = A.aDbuf + (jj & 1) * A.Kp;
+    float* ad_next = A.aDbuf + ((jj + 1) & 1) * A.Kp;
+    const float anorm = S.correct(j, prev, av_cur, ad_cur);
+    const int64_t q0 = A.start[j], cnt = A.start[j + 1] - q0;
+    if (cnt == 0) {
+      if (!S.special_case(j)) return;
+      S.refresh_gp(j, 1.f, false);
+    } else {
+      if (threadIdx.x == 0) use_cnt = 0;
+      __syncthreads();
+      S.update_coefs(j, q0, cnt, anorm, &use_cnt);
+      if (S.c == 0)
+        for (int r = threadIdx.x; r < n; r += blockDim.x) A.D[(int64_t)j * n + r] = S.a_s[r] / anorm;
+      S.refresh_gp(j, 1.f / anorm, true);
+    }
+    if (jn >= 0) {
+      S.next_partials(jn, j, av_next, ad_next);
+      S.zero_row(jn);
+      if (A.start[jn + 1] > A.start[jn]) S.prefetch_next(jn);
+    }
+    if (S.c == 0)
+      for (int r = threadIdx.x; r < n; r += blockDim.x) av_clear[r] = 0.f;
+    if (!S.barrier()) return;
   }
 }
 
@@ -486,11 +714,23 @@ cudaError_t launch_update_prepare(const UpdateArgs& a, cudaStream_t st) {
       a.idx, a.nnz, a.N, a.T, a.K, a.Kp, nblk, a.block_hist, a.start, a.list);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   const size_t psm = sizeof(float) * ((size_t)(kPrepThreads / 32) * (a.Kp + a.n));
-  e = cudaFuncSetAttribute(prepare_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm);
+  const int npl = (a.n + 31) / 32;
+  auto launch = [&](auto kern) -> cudaError_t {
+    cudaError_t e2 = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)psm);
+    if (e2 != cudaSuccess) return e2;
+    kern<<<a.Kp, kPrepThreads, psm, st>>>(a.X, a.n, a.T, a.Kp, a.idx, a.coef, a.nnz, a.list,
+                                          a.start, a.Y, a.gn2, a.C);
+    return cudaGetLastError();
+  };
+  if (npl <= 2) e = launch(prepare_kernel<2>);
+  else if (npl <= 4) e = launch(prepare_kernel<4>);
+  else if (npl <= 8) e = launch(prepare_kernel<8>);
+  else if (npl <= 16) e = launch(prepare_kernel<16>);
+  else e = launch(prepare_kernel<32>);
   if (e != cudaSuccess) return e;
-  prepare_kernel<<<a.Kp, kPrepThreads, psm, st>>>(a.X, a.n, a.T, a.Kp, a.idx, a.coef, a.nnz,
-                                                  a.list, a.start, a.Y, a.gn2, a.C);
-  return cudaGetLastError();
+  // P = D'Y (P(i, j) = d_i . Y_j at P[j*Kp + i])
+  return launch_gemm_tn_f32(a.D, a.n, a.Y, a.n, a.P, a.Kp, a.K, a.Kp, a.K, a.Kp, a.n, st);
 }
 
 cudaError_t launch_update_sweep(const UpdateArgs& a, cudaStream_t st) {
@@ -498,21 +738,30 @@ cudaError_t launch_update_sweep(const UpdateArgs& a, cudaStream_t st) {
   SweepArgs s;
   s.n = a.n; s.K = a.K; s.Kp = a.Kp; s.T = a.T; s.N = a.N; s.X = a.X; s.D = a.D; s.idx = a.idx;
   s.coef = a.coef; s.nnz = a.nnz; s.perm = a.perm; s.max_signals = a.max_signals;
-  s.list = a.list; s.start = a.start; s.Y = a.Y; s.gn2 = a.gn2; s.C = a.C; s.avec = a.avec;
-  s.aD = a.aD; s.part = a.part; s.unused = a.unused; s.bitmap = a.bitmap; s.replaced = a.replaced;
-  s.counter = a.counter; s.usecount = a.usecount; s.barrier = a.barrier; s.dev_err = a.dev_err;
-  const size_t smem = sizeof(float) * ((size_t)a.n + 2 * (size_t)a.Kp);
-  cudaError_t e = cudaFuncSetAttribute(sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
-  if (e != cudaSuccess) return e;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sweep_kernel, kSweepThreads, smem);
-  if (e != cudaSuccess) return e;
-  if (per_sm < 1) return cudaErrorCooperativeLaunchTooLarge;
-  const int grid = sweep_grid_size();
-  void* args[] = {&s};
-  return cudaLaunchCooperativeKernel((const void*)sweep_kernel, dim3(grid), dim3(kSweepThreads),
-                                     args, smem, st);
+  s.list = a.list; s.start = a.start; s.Y = a.Y; s.gn2 = a.gn2; s.C = a.C; s.G = a.G; s.P = a.P;
+  s.avec = a.avec; s.aDbuf = a.aD; s.part = a.part; s.unused = a.unused; s.bitmap = a.bitmap;
+  s.replaced = a.replaced; s.counter = a.counter; s.usecount = a.usecount; s.barrier = a.barrier;
+  s.dev_err = a.dev_err;
+  const size_t smem = sizeof(float) * ((size_t)a.n + 3 * (size_t)a.Kp);
+  const int npl = (a.n + 31) / 32;
+  auto launch = [&](auto kern) -> cudaError_t {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSweepThreads, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorCooperativeLaunchTooLarge;
+    const int grid = sweep_grid_size();
+    void* args[] = {&s};
+    return cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(kSweepThreads), args,
+                                       smem, st);
+  };
+  if (npl <= 2) return launch(sweep_kernel<2>);
+  if (npl <= 4) return launch(sweep_kernel<4>);
+  if (npl <= 8) return launch(sweep_kernel<8>);
+  if (npl <= 16) return launch(sweep_kernel<16>);
+  return launch(sweep_kernel<32>);
 }
 
 int update_sweep_ctas() { return sweep_grid_size(); }

@@ -79,8 +79,14 @@ def _supports(rng, N, K, T, chunk=65536):
     return out
 
 
-def make_problem(cfg, N=None, seed=None, dtype=np.float32, device="cpu"):
+def make_problem(cfg, N=None, seed=None, dtype=np.float32, device="cpu", dict_from="signals"):
     """Returns dict(X=(n,N) col-major, D=(n,K) initial dictionary, D0, support, gamma).
+
+    ``dict_from="signals"`` takes the initial dictionary from K distinct signals of X (the
+    MATLAB toolbox convention the reference's harness follows); ``"extra"`` draws K further
+    signals from the same distribution that are not part of X, so that no signal starts out
+    identical to an atom (used by the parity tests: such a signal's residual is rounding noise
+    after its first atom, and an absolute stop threshold then depends on the arithmetic).
 
     With ``device='cuda'`` X and D are torch CUDA tensors shaped (N, n) and (K, n) row-major,
     i.e. the same column-major memory as the numpy (n, N) / (n, K) arrays."""
@@ -92,6 +98,9 @@ def make_problem(cfg, N=None, seed=None, dtype=np.float32, device="cpu"):
         return _make_problem_torch(cfg, N, seed, device)
     rng = np.random.default_rng(seed)
     D0 = ground_truth_dictionary(cfg, rng)
+    Nx = N
+    if dict_from == "extra":
+        N = N + cfg.K
     sup = _supports(rng, N, cfg.K, cfg.T)
     gam = rng.standard_normal((N, cfg.T))
     X = np.empty((cfg.n, N), dtype=np.float64, order="F")
@@ -103,8 +112,12 @@ def make_problem(cfg, N=None, seed=None, dtype=np.float32, device="cpu"):
         X[:, s0:s1] = clean + rng.standard_normal(clean.shape) * sig
     if cfg.remove_row_mean:
         X -= X.mean(axis=1, keepdims=True)
-    pick = rng.choice(N, size=cfg.K, replace=False)
-    D = _unit_columns(X[:, pick])
+    if dict_from == "extra":
+        D = _unit_columns(X[:, Nx:])
+        X, sup, gam = X[:, :Nx], sup[:Nx], gam[:Nx]
+    else:
+        pick = rng.choice(N, size=cfg.K, replace=False)
+        D = _unit_columns(X[:, pick])
     return dict(X=np.asfortranarray(X.astype(dtype)), D=np.asfortranarray(D.astype(dtype)),
                 D0=D0, support=sup, gamma=gam, cfg=cfg)
 
