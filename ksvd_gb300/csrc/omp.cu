@@ -12,7 +12,8 @@
 // alpha0_I is computed; the earlier entries do not change), the triangular solves run as
 // column sweeps across the lanes that own the support slots, the final alpha update after the
 // last atom is skipped (it is never read), and a failed pivot test does not add the atom.
-// alpha0 is streamed once (evict-first loads); G stays L2-resident.
+// alpha0 is streamed once (evict-first loads); G stays L2-resident, and re-reading the support
+// columns of G from L2 (N*K*T(T-1)/2 floats per sweep of all signals) is what bounds this kernel.
 #include "common.cuh"
 #include "kernels.cuh"
 

@@ -24,7 +24,7 @@ namespace ksvd {
 namespace {
 
 constexpr int kSigPerBlock = 256;      // signals per list-building block
-constexpr int kPrepThreads = 256;
+constexpr int kPrepThreads = 512;
 constexpr int kSweepThreads = 512;
 constexpr unsigned kBarrierSpinLimit = 1u << 24;   // x >= 64 ns sleeps: > 1 s before giving up
 
@@ -182,38 +182,34 @@ prepare_kernel(const float* __restrict__ X, int n, int T, int Kp, const int32_t*
     }
     __syncwarp();
   };
-  int64_t q = q0 + w;
-  for (; q + NW < q1; q += 2 * NW) {
-    const int64_t e0 = list[q], e1 = list[q + NW];
-    const int64_t s0 = e0 / T, s1 = e1 / T;
-    const float ga = coef[e0], gb = coef[e1];
-    const float* xa = X + s0 * n;
-    const float* xb = X + s1 * n;
-    float va[NPL], vb[NPL];
+  constexpr int EB = NPL <= 8 ? 4 : (NPL <= 16 ? 2 : 1);      // entries in flight per warp
+  for (int64_t qs = q0 + (int64_t)w * EB; qs < q1; qs += (int64_t)NW * EB) {
+    const int ne = (int)min((int64_t)EB, q1 - qs);
+    int64_t sg[EB];
+    float gv[EB];
+    float xv[EB][NPL];
 #pragma unroll
-    for (int i = 0; i < NPL; ++i) {
-      const int r = lane + 32 * i;
-      va[i] = r < n ? __ldg(xa + r) : 0.f;
-      vb[i] = r < n ? __ldg(xb + r) : 0.f;
+    for (int b = 0; b < EB; ++b) {
+      const int64_t e = b < ne ? list[qs + b] : 0;
+      sg[b] = e / T;
+      gv[b] = b < ne ? coef[e] : 0.f;
     }
 #pragma unroll
-    for (int i = 0; i < NPL; ++i) acc[i] = fmaf(gb, vb[i], fmaf(ga, va[i], acc[i]));
-    g2 = fmaf(gb, gb, fmaf(ga, ga, g2));
-    scatter(s0, ga);
-    scatter(s1, gb);
-  }
-  if (q < q1) {
-    const int64_t e0 = list[q];
-    const int64_t s0 = e0 / T;
-    const float ga = coef[e0];
-    const float* xa = X + s0 * n;
+    for (int b = 0; b < EB; ++b)
 #pragma unroll
-    for (int i = 0; i < NPL; ++i) {
-      const int r = lane + 32 * i;
-      if (r < n) acc[i] = fmaf(ga, __ldg(xa + r), acc[i]);
+      for (int i = 0; i < NPL; ++i) {
+        const int r = lane + 32 * i;
+        xv[b][i] = (b < ne && r < n) ? __ldg(X + sg[b] * n + r) : 0.f;
+      }
+#pragma unroll
+    for (int b = 0; b < EB; ++b) {
+#pragma unroll
+      for (int i = 0; i < NPL; ++i) acc[i] = fmaf(gv[b], xv[b][i], acc[i]);
+      g2 = fmaf(gv[b], gv[b], g2);
     }
-    g2 = fmaf(ga, ga, g2);
-    scatter(s0, ga);
+#pragma unroll
+    for (int b = 0; b < EB; ++b)
+      if (b < ne) scatter(sg[b], gv[b]);
   }
 #pragma unroll
   for (int i = 0; i < NPL; ++i) {
@@ -364,7 +360,9 @@ struct Sweep {
 
   __device__ bool barrier() { return grid_barrier(A.barrier, nctas, A.dev_err, sflag); }
 
-  // Slices of a'(jn) and a'(jn)'D leaving out atom jx (jx = -1: nothing left out).
+  // Slices of a'(jn) and a'(jn)'D leaving out atom jx (jx = -1: nothing left out).  The left-out
+  // atom gets weight 0 in v_s; its column of D and entry of G may be rewritten concurrently by
+  // this phase, but any value read there is finite and is multiplied by that 0.
   __device__ void next_partials(int jn, int jx, float* avec_slot, float* aD_slot) {
     const int n = A.n, K = A.K, Kp = A.Kp;
     const float g2 = A.gn2[jn];
@@ -374,19 +372,27 @@ struct Sweep {
     if (k1 > k0 || c == 0) {
       for (int r = tid; r < n; r += blockDim.x) {
         float acc = 0.f;
-#pragma unroll 4
-        for (int k = k0; k < k1; ++k)
-          if (k != jx) acc = fmaf(-v_s[k], __ldcg(A.D + (int64_t)k * n + r), acc);
+#pragma unroll 8
+        for (int k = k0; k < k1; ++k) acc = fmaf(-v_s[k], __ldcg(A.D + (int64_t)k * n + r), acc);
         if (c == 0) acc += A.Y[(int64_t)jn * n + r] + g2 * __ldcg(A.D + (int64_t)jn * n + r);
         atomicAdd(avec_slot + r, acc);
       }
     }
+    const int k4n = Kp >> 2;                          // Kp is a multiple of 128
     for (int i = k0 + w; i < k1; i += NW) {
       if (i == jx) continue;
-      const float* gi = A.G + (int64_t)i * Kp;       // column i of G = row i
+      const float4* gi = reinterpret_cast<const float4*>(A.G + (int64_t)i * Kp);
+      const float4* vv = reinterpret_cast<const float4*>(v_s);
       float acc = 0.f;
-      for (int k = lane; k < K; k += 32)
-        if (k != jx) acc = fmaf(__ldcg(gi + k), v_s[k], acc);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {                   // Kp <= 1024: at most 8 float4 per lane
+        const int k4 = lane + 32 * u;
+        if (k4 < k4n) {
+          const float4 g = __ldcg(gi + k4);
+          const float4 v = vv[k4];
+          acc = fmaf(g.x, v.x, fmaf(g.y, v.y, fmaf(g.z, v.z, fmaf(g.w, v.w, acc))));
+        }
+      }
       acc = warp_sum(acc);
       if (lane == 0)
         aD_slot[i] = __ldcg(A.P + (int64_t)jn * Kp + i) - acc +
@@ -408,6 +414,7 @@ struct Sweep {
       float g, pj;
       const float* yi = A.Y + (int64_t)i * n;
       float accp = 0.f, accg = 0.f;
+#pragma unroll 8
       for (int r = lane; r < n; r += 32) {
         accp = fmaf(a_s[r], __ldg(yi + r), accp);
         if (!from_aD) accg = fmaf(a_s[r], __ldcg(A.D + (int64_t)i * n + r), accg);
@@ -445,6 +452,7 @@ struct Sweep {
       cpart[i] = 0.f;
     }
     float dp = 0.f, nn = 0.f;
+#pragma unroll 2
     for (int r = tid; r < n; r += blockDim.x) {
       nn = fmaf(a_s[r], a_s[r], nn);
       if (prev >= 0) dp = fmaf(__ldcg(A.D + (int64_t)prev * n + r), a_s[r], dp);
