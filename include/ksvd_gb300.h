@@ -195,6 +195,22 @@ KSVD_API ksvd_status ksvd_dense_gamma(ksvd_handle* handle, int64_t N, const int3
 KSVD_API ksvd_status ksvd_read_stage_times(ksvd_handle* handle, ksvd_stage_times* out,
                                            int32_t reset);
 
+/* sqrt(sum_s ||x_s - D gamma_s||^2 / (n N)) -- the RMSE of ksvd_error -- without allocating any
+ * device memory and without a handle, for callers that cannot call cudaMalloc where they need
+ * the number: their device memory is owned by another allocator (a framework's caching
+ * allocator, a fixed budget given to a plugin), or they run on a latency-critical path where
+ * cudaMalloc's implicit device synchronisation is not acceptable.  All arrays are DEVICE arrays
+ * (D n x K, X n x N, the sparse code); *rmse is written on the HOST and the stream is
+ * synchronised.  The scratch is a static device array of 65,538 doubles: N <= 16,777,216
+ * (KSVD_ERR_UNSUPPORTED beyond), n <= 1024, K <= 1024, T <= 64.  The first call on a device
+ * resolves the array's address (make it before any stream capture); concurrent calls on one
+ * device race on the shared array.  ksvd_last_error(NULL) describes the last failure.  No
+ * counterpart in the reference. */
+KSVD_API ksvd_status ksvd_rmse_noalloc(int32_t n, int32_t K, int32_t T, const float* D,
+                                       const float* X, int64_t N, const int32_t* idx,
+                                       const float* coef, const int32_t* nnz, double* rmse,
+                                       void* stream);
+
 /* Block until all work enqueued by this handle has finished; reports device-side errors. */
 KSVD_API ksvd_status ksvd_synchronize(ksvd_handle* handle);
 

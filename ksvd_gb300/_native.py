@@ -30,6 +30,7 @@ EXPORTS = (
     "ksvd_normcols", "ksvd_gram", "ksvd_dtx", "ksvd_omp_gram", "ksvd_omp",
     "ksvd_update_dictionary", "ksvd_error", "ksvd_clear_dict", "ksvd_iterate",
     "ksvd_iterate_host", "ksvd_dense_gamma", "ksvd_synchronize", "ksvd_read_stage_times",
+    "ksvd_rmse_noalloc",
 )
 
 FLAG_PROFILE = 1
@@ -86,6 +87,8 @@ def _declare(lib):
         "ksvd_dense_gamma": (st, [vp, i64, vp, vp, vp, vp]),
         "ksvd_synchronize": (st, [vp]),
         "ksvd_read_stage_times": (st, [vp, C.POINTER(StageTimes), i32]),
+        "ksvd_rmse_noalloc": (st, [i32, i32, i32, vp, vp, i64, vp, vp, vp, C.POINTER(C.c_double),
+                                   vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -433,7 +433,11 @@ const char* ksvd_status_string(ksvd_status s) {
   return "unknown status";
 }
 
-const char* ksvd_last_error(const ksvd_handle* h) { return h ? h->err.c_str() : ""; }
+const char* ksvd_noalloc_last_error();
+
+const char* ksvd_last_error(const ksvd_handle* h) {
+  return h ? h->err.c_str() : ksvd_noalloc_last_error();
+}
 
 int64_t ksvd_workspace_bytes(const ksvd_handle* h) {
   if (!h) return 0;
