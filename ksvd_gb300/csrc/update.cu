@@ -331,12 +331,13 @@ struct SweepArgs {
 template <int NPL>
 struct Sweep {
   static constexpr int NW = kSweepThreads / 32;
+  static constexpr int HALF = kSweepThreads / 2;                  // threads per warp group
   static constexpr int EB = NPL <= 8 ? 4 : (NPL <= 16 ? 2 : 1);   // entries per warp batch
   const SweepArgs& A;
   float* a_s;      // n     current atom vector a(j)
   float* aD_s;     // Kp    a(j)'D
   float* cpart;    // Kp    this CTA's part of the new row j of C
-  float* v_s;      // Kp    C(:, j') for the next atom
+  float* v_s;      // Kp    C(:, j') for the next atom (its left-out entry 0)
   float* red_f;
   int* red_i;
   int* sflag;
@@ -360,17 +361,21 @@ struct Sweep {
 
   __device__ bool barrier() { return grid_barrier(A.barrier, nctas, A.dev_err, sflag); }
 
-  // Slices of a'(jn) and a'(jn)'D leaving out atom jx (jx = -1: nothing left out).  The left-out
-  // atom gets weight 0 in v_s; its column of D and entry of G may be rewritten concurrently by
-  // this phase, but any value read there is finite and is multiplied by that 0.
-  __device__ void next_partials(int jn, int jx, float* avec_slot, float* aD_slot) {
-    const int n = A.n, K = A.K, Kp = A.Kp;
+  __device__ float v_entry(int k, int jn, int jx) const {
+    return (k >= A.K || k == jx) ? 0.f
+                                 : (k == jn ? A.gn2[jn] : __ldcg(A.C + (int64_t)jn * A.Kp + k));
+  }
+
+  // Slices of a'(jn) and a'(jn)'D leaving out atom jx, from v_s (loaded and synchronised by
+  // the caller), by the threads [gt0, gt0 + gsize) of this CTA.  The left-out atom has weight 0
+  // in v_s; its column of D and entry of G may be rewritten concurrently by this phase, but any
+  // value read there is finite and is multiplied by that 0.
+  __device__ void next_partials(int jn, int jx, float* avec_slot, float* aD_slot, int gt,
+                                int gsize) {
+    const int n = A.n, Kp = A.Kp;
     const float g2 = A.gn2[jn];
-    for (int k = tid; k < Kp; k += blockDim.x)
-      v_s[k] = (k >= K || k == jx) ? 0.f : (k == jn ? g2 : __ldcg(A.C + (int64_t)jn * Kp + k));
-    __syncthreads();
     if (k1 > k0 || c == 0) {
-      for (int r = tid; r < n; r += blockDim.x) {
+      for (int r = gt; r < n; r += gsize) {
         float acc = 0.f;
 #pragma unroll 8
         for (int k = k0; k < k1; ++k) acc = fmaf(-v_s[k], __ldcg(A.D + (int64_t)k * n + r), acc);
@@ -379,8 +384,9 @@ struct Sweep {
       }
     }
     const int k4n = Kp >> 2;                          // Kp is a multiple of 128
-    for (int i = k0 + w; i < k1; i += NW) {
-      if (i == jx) continue;
+    const int gw = gt >> 5, gnw = gsize >> 5;
+    for (int i = k0 + gw; i < k1; i += gnw) {
+      if (i == jx) continue;                          // a(jn)'d_jx is formed after the barrier
       const float4* gi = reinterpret_cast<const float4*>(A.G + (int64_t)i * Kp);
       const float4* vv = reinterpret_cast<const float4*>(v_s);
       float acc = 0.f;
@@ -401,17 +407,17 @@ struct Sweep {
   }
 
   // Row jn of C is rebuilt by atom jn's phase: clear this CTA's slice of it.
-  __device__ void zero_row(int jn) {
-    for (int k = k0 + tid; k < k1; k += blockDim.x) A.C[(int64_t)k * A.Kp + jn] = 0.f;
+  __device__ void zero_row(int jn, int gt, int gsize) {
+    for (int k = k0 + gt; k < k1; k += gsize) A.C[(int64_t)k * A.Kp + jn] = 0.f;
   }
 
-  // Atom j's new column d_j is in D: G(:, j), G(j, :), P(j, :) for this CTA's slice.
-  // scale = 1/||a|| when a_s holds the unnormalised atom (regular path) -- then G comes from
-  // aD_s -- or 0 when a_s already holds d_j (special case) and G is recomputed from D.
-  __device__ void refresh_gp(int j, float inv_norm, bool from_aD) {
+  // G(:, j), G(j, :) and P(j, :) for this CTA's atom slice once d_j is final.  Regular path:
+  // a_s holds the unnormalised atom and G(i, j) = a'd_i / ||a|| comes from aD_s.  Special case:
+  // a_s holds d_j and G(i, j) is recomputed from D.
+  __device__ void refresh_gp(int j, float inv_norm, bool from_aD, int gt, int gsize) {
     const int n = A.n, Kp = A.Kp;
-    for (int i = k0 + w; i < k1; i += NW) {
-      float g, pj;
+    const int gw = gt >> 5, gnw = gsize >> 5;
+    for (int i = k0 + gw; i < k1; i += gnw) {
       const float* yi = A.Y + (int64_t)i * n;
       float accp = 0.f, accg = 0.f;
 #pragma unroll 8
@@ -421,58 +427,77 @@ struct Sweep {
       }
       accp = warp_sum(accp);
       if (!from_aD) accg = warp_sum(accg);
-      pj = accp * inv_norm;
-      g = from_aD ? aD_s[i] * inv_norm : accg * inv_norm;
+      float g = from_aD ? aD_s[i] * inv_norm : accg * inv_norm;
       if (i == j) g = 1.f;
       if (lane == 0) {
         A.G[(int64_t)j * Kp + i] = g;
         A.G[(int64_t)i * Kp + j] = g;
-        A.P[(int64_t)i * Kp + j] = pj;
+        A.P[(int64_t)i * Kp + j] = accp * inv_norm;
       }
     }
   }
 
-  // Fold the left-out atom prev back into a(j) and a(j)'D; returns ||a(j)||.
-  __device__ float correct(int j, int prev, const float* avec_slot, const float* aD_slot) {
+  // Fold the left-out atom prev back into a(j) and a(j)'D, and load v_s for the next atom jn
+  // (leaving out j): every load of the phase's start in one round.  Returns ||a(j)||.
+  __device__ float correct(int j, int prev, int jn, const float* avec_slot, const float* aD_slot) {
     const int n = A.n, K = A.K, Kp = A.Kp;
     const float cp = prev >= 0 ? __ldcg(A.C + (int64_t)j * Kp + prev) : 0.f;
-    for (int r = tid; r < n; r += blockDim.x) {
-      float v = __ldcg(avec_slot + r);
-      if (prev >= 0) v = fmaf(-cp, __ldcg(A.D + (int64_t)prev * n + r), v);
-      a_s[r] = v;
+    float av[2], dv[2], ad[2], gp[2], vn[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {                     // n, Kp <= 1024 = 2 x 512 threads
+      const int r = tid + u * kSweepThreads;
+      av[u] = r < n ? __ldcg(avec_slot + r) : 0.f;
+      dv[u] = (r < n && prev >= 0) ? __ldcg(A.D + (int64_t)prev * n + r) : 0.f;
+      const int i = r;
+      const bool ok = i < K && i != prev;
+      ad[u] = ok ? __ldcg(aD_slot + i) : 0.f;
+      gp[u] = (ok && prev >= 0) ? __ldcg(A.G + (int64_t)prev * Kp + i) : 0.f;
+      vn[u] = (jn >= 0 && i < Kp) ? v_entry(i, jn, j) : 0.f;
     }
-    __syncthreads();
-    for (int i = tid; i < Kp; i += blockDim.x) {
-      float v = 0.f;
-      if (i < K && i != prev) {
-        v = __ldcg(aD_slot + i);
-        if (prev >= 0) v = fmaf(-cp, __ldcg(A.G + (int64_t)prev * Kp + i), v);
+    float nn = 0.f, dp = 0.f;
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int r = tid + u * kSweepThreads;
+      if (r < n) {
+        const float a = fmaf(-cp, dv[u], av[u]);
+        a_s[r] = a;
+        nn = fmaf(a, a, nn);
+        dp = fmaf(dv[u], a, dp);
       }
-      aD_s[i] = v;
-      cpart[i] = 0.f;
+      if (r < Kp) {
+        aD_s[r] = fmaf(-cp, gp[u], ad[u]);
+        cpart[r] = 0.f;
+        v_s[r] = vn[u];
+      }
     }
-    float dp = 0.f, nn = 0.f;
-#pragma unroll 2
-    for (int r = tid; r < n; r += blockDim.x) {
-      nn = fmaf(a_s[r], a_s[r], nn);
-      if (prev >= 0) dp = fmaf(__ldcg(A.D + (int64_t)prev * n + r), a_s[r], dp);
-    }
-    nn = block_sum(nn, red_f);
-    if (prev >= 0) {
-      dp = block_sum(dp, red_f);
-      if (tid == 0) aD_s[prev] = dp;
+    nn = warp_sum(nn);
+    dp = warp_sum(dp);
+    if (lane == 0) { red_f[w] = nn; red_f[32 + w] = dp; }
+    __syncthreads();
+    if (w == 0) {
+      nn = lane < NW ? red_f[lane] : 0.f;
+      dp = lane < NW ? red_f[32 + lane] : 0.f;
+      nn = warp_sum(nn);
+      dp = warp_sum(dp);
+      if (lane == 0) {
+        red_f[0] = nn;
+        if (prev >= 0) aD_s[prev] = dp;
+      }
     }
     __syncthreads();
-    return sqrtf(nn);
+    const float anorm = sqrtf(red_f[0]);
+    __syncthreads();
+    return anorm;
   }
 
   // Issue L2 prefetches of the signals (and their codes) the next atom will read.
-  __device__ void prefetch_next(int jn) {
+  __device__ void prefetch_next(int jn, int gt, int gsize) {
     const int64_t q0 = A.start[jn], cnt = A.start[jn + 1] - q0;
+    if (cnt == 0) return;
     const int64_t per = (cnt + nctas - 1) / nctas;
     const int64_t qa = q0 + min(cnt, (int64_t)c * per), qb = q0 + min(cnt, (int64_t)(c + 1) * per);
     const bool bulk_x = (A.n & 3) == 0, bulk_c = (A.T & 3) == 0;
-    for (int64_t q = qa + tid; q < qb; q += blockDim.x) {
+    for (int64_t q = qa + gt; q < qb; q += gsize) {
       const int64_t s = A.list[q] / A.T;
       const float* x = A.X + s * A.n;
       if (bulk_x) prefetch_l2_bulk(x, (uint32_t)A.n * 4);
@@ -483,14 +508,16 @@ struct Sweep {
     }
   }
 
-  // New coefficients of atom j for this CTA's share of its signals; C row j and use count.
-  __device__ void update_coefs(int j, int64_t q0, int64_t cnt, float anorm, int* use_cnt) {
+  // New coefficients of atom j for this CTA's share of its signals, by warps [0, gnw).  Adds
+  // into cpart (C row j) and *use_cnt; the caller synchronises and flushes.
+  __device__ void update_coefs(int j, int64_t q0, int64_t cnt, float anorm, int gw, int gnw,
+                               int* use_cnt) {
     const int n = A.n, K = A.K, T = A.T;
     const float aDj = aD_s[j];
     const int64_t per = (cnt + nctas - 1) / nctas;
     const int64_t qa = q0 + min(cnt, (int64_t)c * per), qb = q0 + min(cnt, (int64_t)(c + 1) * per);
     int my_use = 0;
-    for (int64_t qs = qa + (int64_t)w * EB; qs < qb; qs += (int64_t)NW * EB) {
+    for (int64_t qs = qa + (int64_t)gw * EB; qs < qb; qs += (int64_t)gnw * EB) {
       const int ne = (int)min((int64_t)EB, qb - qs);
       int64_t e[EB], s[EB];
       int nz[EB];
@@ -558,8 +585,11 @@ struct Sweep {
       }
     }
     if (lane == 0 && my_use) atomicAdd(use_cnt, my_use);
-    __syncthreads();
-    for (int k = tid; k < K; k += blockDim.x) {
+  }
+
+  // After a CTA barrier: this CTA's part of C row j and of atom j's use count.
+  __device__ void flush_row(int j, const int* use_cnt) {
+    for (int k = tid; k < A.K; k += blockDim.x) {
       const float v = cpart[k];
       if (k != j && v != 0.f) atomicAdd(A.C + (int64_t)k * A.Kp + j, v);
     }
@@ -640,54 +670,66 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
   __shared__ int sflag;
   __shared__ int use_cnt;
   Sweep<NPL> S(A, sm, red_f, red_i, &sflag);
-  const int K = A.K, n = A.n;
+  const int K = A.K, n = A.n, tid = threadIdx.x;
+  constexpr int HALF = Sweep<NPL>::HALF;
   // every CTA checks the whole permutation itself, so all of them leave together or none does
   int bad = 0;
-  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+  for (int k = tid; k < K; k += blockDim.x) {
     const int j = A.perm[k];
     bad |= (j < 0 || j >= K);
   }
   if (__syncthreads_or(bad)) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(A.dev_err, kDevErrBounds);
+    if (blockIdx.x == 0 && tid == 0) atomicOr(A.dev_err, kDevErrBounds);
     return;
   }
   // prologue: a(perm[0]) and a(perm[0])'D in full
   {
     const int j0 = A.perm[0];
-    S.zero_row(j0);
-    S.next_partials(j0, -1, A.avec, A.aDbuf);
-    if (A.start[j0 + 1] > A.start[j0]) S.prefetch_next(j0);
+    for (int k = tid; k < A.Kp; k += blockDim.x) S.v_s[k] = S.v_entry(k, j0, -1);
+    __syncthreads();
+    S.next_partials(j0, -1, A.avec, A.aDbuf, tid, blockDim.x);
+    S.zero_row(j0, tid, blockDim.x);
+    S.prefetch_next(j0, tid, blockDim.x);
     if (!S.barrier()) return;
   }
   for (int jj = 0; jj < K; ++jj) {
     const int j = A.perm[jj];
     const int prev = jj > 0 ? A.perm[jj - 1] : -1;
     const int jn = jj + 1 < K ? A.perm[jj + 1] : -1;
-    float* av_cur = A.avec + (jj % 3) * n;
     float* av_next = A.avec + ((jj + 1) % 3) * n;
     float* av_clear = A.avec + ((jj + 2) % 3) * n;
-    const float* ad_cur = A.aDbuf + (jj & 1) * A.Kp;
     float* ad_next = A.aDbuf + ((jj + 1) & 1) * A.Kp;
-    const float anorm = S.correct(j, prev, av_cur, ad_cur);
+    if (tid == 0) use_cnt = 0;
+    const float anorm = S.correct(j, prev, jn, A.avec + (jj % 3) * n, A.aDbuf + (jj & 1) * A.Kp);
     const int64_t q0 = A.start[j], cnt = A.start[j + 1] - q0;
     if (cnt == 0) {
+      // special case: all warps, then the next atom's partials
       if (!S.special_case(j)) return;
-      S.refresh_gp(j, 1.f, false);
+      S.refresh_gp(j, 1.f, false, tid, blockDim.x);
+      if (jn >= 0) {
+        S.next_partials(jn, j, av_next, ad_next, tid, blockDim.x);
+        S.zero_row(jn, tid, blockDim.x);
+        S.prefetch_next(jn, tid, blockDim.x);
+      }
+    } else if (tid < HALF) {
+      // warps 0..7: atom j's new coefficients
+      S.update_coefs(j, q0, cnt, anorm, tid >> 5, HALF >> 5, &use_cnt);
     } else {
-      if (threadIdx.x == 0) use_cnt = 0;
-      __syncthreads();
-      S.update_coefs(j, q0, cnt, anorm, &use_cnt);
+      // warps 8..15: d_j, G/P rows of j, the next atom's partials, prefetch
+      const int gt = tid - HALF;
       if (S.c == 0)
-        for (int r = threadIdx.x; r < n; r += blockDim.x) A.D[(int64_t)j * n + r] = S.a_s[r] / anorm;
-      S.refresh_gp(j, 1.f / anorm, true);
+        for (int r = gt; r < n; r += HALF) A.D[(int64_t)j * n + r] = S.a_s[r] / anorm;
+      S.refresh_gp(j, 1.f / anorm, true, gt, HALF);
+      if (jn >= 0) {
+        S.next_partials(jn, j, av_next, ad_next, gt, HALF);
+        S.zero_row(jn, gt, HALF);
+        S.prefetch_next(jn, gt, HALF);
+      }
     }
-    if (jn >= 0) {
-      S.next_partials(jn, j, av_next, ad_next);
-      S.zero_row(jn);
-      if (A.start[jn + 1] > A.start[jn]) S.prefetch_next(jn);
-    }
+    __syncthreads();
+    if (cnt > 0) S.flush_row(j, &use_cnt);
     if (S.c == 0)
-      for (int r = threadIdx.x; r < n; r += blockDim.x) av_clear[r] = 0.f;
+      for (int r = tid; r < n; r += blockDim.x) av_clear[r] = 0.f;
     if (!S.barrier()) return;
   }
 }
