@@ -33,8 +33,11 @@ if ROOT not in sys.path:
 # Gram; mixed adds the D split for the Gram and the X split) and per iteration (D'X, OMP, six
 # list/precompute kernels, sweep, error, RMSE, Gram, coherence, clearDict; mixed adds two
 # dictionary splits)
+# library kernels per ksvd_iterate call: copy_pad_cols, normcols, Gram (mixed: + BF16 splits of D
+# and X); per iteration: D'X, OMP, Gram, 4 list kernels, init_state, prepare, P = D'Y, sweep,
+# error + rmse, Gram, coherence + clear_seq, advance_counter (mixed: + 3 BF16 splits of D)
 KERNELS_PER_CALL = {"fp32": 3, "mixed": 5}
-KERNELS_PER_ITER = {"fp32": 14, "mixed": 16}
+KERNELS_PER_ITER = {"fp32": 17, "mixed": 20}
 
 
 def peaks():
@@ -116,12 +119,23 @@ def stage_bytes(cfg, N, stage):
 
 
 def stage_flops(cfg, N, stage):
-    n, K = cfg.n, cfg.K
+    n, K, T = cfg.n, cfg.K, cfg.T
     if stage == "dtx":
         return 2.0 * n * K * N
     if stage == "gram":
         return 2.0 * n * K * K
+    if stage == "omp":      # alpha updates: sum over steps t of 2*K*t  (= K*T(T+1) per signal)
+        return float(N) * K * T * (T + 1)
     return 0.0
+
+
+# DRAM bytes per signal of one launch, from ncu captures (dram__bytes_read.sum +
+# dram__bytes_write.sum) of the same kernel on 100,000 signals of the same (n, K, T); traffic grows
+# in proportion to the signals, so the bench scales it to its N.  profiles/omp_kernel_cfg2.md.
+MEASURED_TRAFFIC = {("omp", 256, 1024, 16): (414.642432e6 + 7.440128e6) / 100_000}
+
+# FP32 CUDA-core peak (nominal): 152 SMs x 128 FMA lanes x 2 FLOP x 2.07 GHz.
+FP32_SIMT_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 
 
 def dist_env():
@@ -210,6 +224,8 @@ def main():
                     help="override N (smaller cases for profiler captures)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="time plain launches instead of CUDA-graph replays of the iteration")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -245,11 +261,13 @@ def main():
                                 seed=datagen.SEED_BASE + cfg.index + 1000 * rank, device="cuda")
     X, D = prob["X"], prob["D"]
     N = X.shape[0]
-    h = Handle(cfg.n, cfg.K, cfg.T, precision=args.precision, profile=True)
+    # timed handle: iterations 2..K of each call replay a CUDA graph of one iteration;
+    # a second, profiling handle measures per-stage times (events) in a separate pass
+    h = Handle(cfg.n, cfg.K, cfg.T, precision=args.precision, graph=not args.no_graph)
+    hp = Handle(cfg.n, cfg.K, cfg.T, precision=args.precision, profile=True)
     idx, coef, nnz = h._code(N, dev)
     out = (idx, coef, nnz)
     rms = list(h.iterate(D, X, args.warmup, out=out)[3])
-    h.stage_times(reset=True)
     sampler = ClockSampler(local)
     if dist:
         dist.barrier()
@@ -269,8 +287,12 @@ def main():
         t = torch.tensor([ms], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    st = h.stage_times()
     value = ws * args.steps / (ms / 1e3)
+    replays = h.graph_replays()
+    hp.iterate(D, X, 1, out=out)                  # warm the profiling handle's workspace
+    hp.stage_times(reset=True)
+    hp.iterate(D, X, min(args.steps, 5), out=out)
+    st = hp.stage_times()
 
     # dominant stage and its roofline (per-launch device time from events on the kernels' stream)
     pk = peaks()
@@ -285,6 +307,16 @@ def main():
         ach = stage_bytes(cfg, N, dom) / (launch_ms / 1e3) / 1e9
         roof = {"bound": "hbm", "achieved": ach, "peak": pk["hbm"], "unit": "GB/s",
                 "frac": ach / pk["hbm"], "traffic": None}
+    tpu = MEASURED_TRAFFIC.get((dom, cfg.n, cfg.K, cfg.T))
+    if tpu is not None and roof["bound"] == "hbm":
+        roof["traffic"] = tpu * N
+        roof["traffic_source"] = "ncu capture at N=100000, scaled by N"
+    fl = stage_flops(cfg, N, dom)
+    if dom == "omp" and fl > 0:
+        # the OMP step's alpha updates also have a compute roof (FP32 CUDA cores)
+        tf = fl / (launch_ms / 1e3) / 1e12
+        roof["compute"] = {"achieved": tf, "peak": FP32_SIMT_TFLOPS, "unit": "TFLOP/s",
+                           "frac": tf / FP32_SIMT_TFLOPS, "peak_source": "nominal FP32 SIMT"}
     roof["kernel"] = dom
     roof["peak_source"] = pk["src"]
     stage_summary = {k: {"ms_per_launch": round(v[0], 4), "share": round(v[0] * v[1] / sum(
@@ -332,6 +364,8 @@ def main():
                        % (cfg.name, cfg.n, cfg.K, N, cfg.T), "n": cfg.n, "K": cfg.K, "N": N,
                        "T": cfg.T, "precision": args.precision,
                        "parallelism": "replicas%d" % ws if ws > 1 else "single",
+                       "cuda_graph": {"enabled": not args.no_graph,
+                                      "replayed_iterations": replays},
                        "l2": "inputs larger than L2 (X = %.2f GB)" % (X.numel() * 4 / 1e9)},
             "omp_signals_per_s": {"value": ws * N / (omp_ms / 1e3) if omp_ms else None,
                                   "unit": "signals/s", "stages": "D'X + Batch-OMP"},
@@ -347,6 +381,7 @@ def main():
         }
         print(json.dumps(line), flush=True)
     h.close()
+    hp.close()
     if dist:
         dist.destroy_process_group()
     return 0

@@ -78,6 +78,13 @@ typedef struct ksvd_handle ksvd_handle;
 
 /* params.flags bits */
 #define KSVD_FLAG_PROFILE 1  /* record per-stage device time (CUDA events on the handle's stream) */
+#define KSVD_FLAG_REFINE_FINAL 2 /* ksvd_iterate ends with ksvd_refine_coefs on the final D:
+                                    the returned coefficients are then the least-squares ones on
+                                    the final supports (the reference returns the sweep's) */
+#define KSVD_FLAG_GRAPH 4        /* ksvd_iterate captures one K-SVD iteration in a CUDA graph and
+                                    replays it for iterations 2..iters (on a private stream,
+                                    fenced to the handle's stream); the graph is cached while
+                                    the buffers stay the same.  Ignored with KSVD_FLAG_PROFILE. */
 
 /* Stages of one K-SVD iteration, for ksvd_read_stage_times(). */
 typedef enum ksvd_stage {
@@ -165,6 +172,64 @@ KSVD_API ksvd_status ksvd_error(ksvd_handle* handle, const float* D, const float
 KSVD_API ksvd_status ksvd_clear_dict(ksvd_handle* handle, float* D, const float* X, int64_t N,
                             const int32_t* idx, const float* coef, const int32_t* nnz,
                             int32_t* cleared);
+
+/* Fixed-support coding, the differentiable form of the coding step: for every signal the least
+ * squares coefficients on the support given by idx/nnz (T slots per signal, e.g. from ksvd_omp),
+ * gamma_S = (D_S'D_S)^-1 D_S'x.  chol (nullable) receives each signal's lower Cholesky factor of
+ * D_S'D_S, packed row by row, T(T+1)/2 floats per signal, for ksvd_code_backward.  coef gets the
+ * coefficients (0 in unused slots).  No counterpart in the reference (its coding is OMP only). */
+KSVD_API ksvd_status ksvd_code_fixed(ksvd_handle* handle, const float* D, const float* X, int64_t N,
+                                     const int32_t* idx, const int32_t* nnz, float* coef,
+                                     float* chol);
+
+/* One step of mixed-precision iterative refinement of least-squares coefficients on the fixed
+ * supports idx/nnz: r = x - D_S gamma accumulated in FP64, delta = (D_S'D_S)^-1 D_S'r with the FP32
+ * Cholesky factor, gamma += delta.  coef (N x T slots) is updated in place, rounded to FP32;
+ * coef64 (nullable, N x T doubles) receives the FP64 result.  Starting from any coefficients on
+ * the support this gives the least-squares solution to ~(cond * 2^-24)^2 relative error.
+ * No counterpart in the reference (its coefficients are never refined). */
+KSVD_API ksvd_status ksvd_refine_coefs(ksvd_handle* handle, const float* D, const float* X,
+                                       int64_t N, const int32_t* idx, const int32_t* nnz,
+                                       float* coef, double* coef64);
+
+/* Adjoint of ksvd_code_fixed: given dcoef = dL/dgamma (T slots per signal), adds the gradient
+ * through the coding step, dL/dD(:, S_t) += r u_t - (D_S u) gamma_t with u = (D_S'D_S)^-1 dcoef
+ * and r = x - D_S gamma, into dD (n x K, accumulated: zero it for a fresh gradient; nullable),
+ * and writes dL/dX = D_S u into dX (n x N; nullable).  Uses the Cholesky factors saved by
+ * ksvd_code_fixed.  No counterpart in the reference. */
+KSVD_API ksvd_status ksvd_code_backward(ksvd_handle* handle, const float* D, const float* X,
+                                        int64_t N, const int32_t* idx, const int32_t* nnz,
+                                        const float* coef, const float* chol, const float* dcoef,
+                                        float* dD, float* dX);
+
+/* Number of iterations ksvd_iterate has run as CUDA-graph replays on this handle (0 when the
+ * flag is off or capture was refused, in which case the iterations ran as plain launches). */
+KSVD_API int64_t ksvd_graph_replays(const ksvd_handle* handle);
+
+/* ---- many independent problems ------------------------------------------------------------- */
+
+/* One problem of a batched call.  Device pointers, column-major like the single-problem calls. */
+typedef struct ksvd_problem {
+  int32_t n;          /* signal length, 1..1024                                              */
+  int32_t K;          /* atoms, 1..1024                                                      */
+  int32_t T;          /* coefficient slots per signal (maximum support), 1..min(K, 64)        */
+  int32_t reserved;   /* 0                                                                   */
+  int64_t N;          /* signals (0 = skip this problem)                                     */
+  float* D;           /* n x K dictionary, unit-norm columns (ksvd_batched_iterate updates it) */
+  const float* X;     /* n x N signals                                                       */
+  const float* eps2;  /* N error targets ||x - D gamma||^2 <= eps2 (nullable: T atoms each)   */
+  int32_t* idx;       /* N x T atom slots (out)                                              */
+  float* coef;        /* N x T coefficients (out)                                            */
+  int32_t* nnz;       /* N atoms used per signal (out)                                       */
+} ksvd_problem;
+
+/* Batch-OMP of every problem: one grouped GEMM launch for all G = D'D and alpha0 = D'X, then ONE
+ * persistent launch in which warps take chunks of signals of any problem from a device work
+ * queue (uneven supports from the error targets balance themselves).  FP32; the handle's
+ * n/K/T are not used, only its stream and workspace.  Asynchronous on the handle's stream.
+ * Replaces a loop of OMP::BatchOMP calls (S/OMP.cu:42-59), one per dictionary. */
+KSVD_API ksvd_status ksvd_batched_omp(ksvd_handle* handle, const ksvd_problem* probs,
+                                      int32_t nprob);
 
 /* ---- whole algorithm ----------------------------------------------------------------------- */
 

@@ -30,10 +30,13 @@ EXPORTS = (
     "ksvd_normcols", "ksvd_gram", "ksvd_dtx", "ksvd_omp_gram", "ksvd_omp",
     "ksvd_update_dictionary", "ksvd_error", "ksvd_clear_dict", "ksvd_iterate",
     "ksvd_iterate_host", "ksvd_dense_gamma", "ksvd_synchronize", "ksvd_read_stage_times",
-    "ksvd_rmse_noalloc",
+    "ksvd_rmse_noalloc", "ksvd_code_fixed", "ksvd_code_backward",
+    "ksvd_refine_coefs", "ksvd_batched_omp", "ksvd_graph_replays",
 )
 
 FLAG_PROFILE = 1
+FLAG_REFINE_FINAL = 2
+FLAG_GRAPH = 4
 STAGES = ("gram", "dtx", "omp", "lists", "sweep", "error", "clear")
 
 
@@ -47,6 +50,13 @@ class Params(C.Structure):
         ("mu_thresh", C.c_float), ("use_thresh", C.c_int32),
         ("max_replace_signals", C.c_int32), ("flags", C.c_int32), ("seed", C.c_uint64),
     ]
+
+
+class Problem(C.Structure):
+    """ksvd_problem: one problem of a batched call (device pointers)."""
+    _fields_ = [("n", C.c_int32), ("K", C.c_int32), ("T", C.c_int32), ("reserved", C.c_int32),
+                ("N", C.c_int64), ("D", C.c_void_p), ("X", C.c_void_p), ("eps2", C.c_void_p),
+                ("idx", C.c_void_p), ("coef", C.c_void_p), ("nnz", C.c_void_p)]
 
 
 class KsvdError(RuntimeError):
@@ -89,6 +99,11 @@ def _declare(lib):
         "ksvd_read_stage_times": (st, [vp, C.POINTER(StageTimes), i32]),
         "ksvd_rmse_noalloc": (st, [i32, i32, i32, vp, vp, i64, vp, vp, vp, C.POINTER(C.c_double),
                                    vp]),
+        "ksvd_code_fixed": (st, [vp, vp, vp, i64, vp, vp, vp, vp]),
+        "ksvd_code_backward": (st, [vp, vp, vp, i64, vp, vp, vp, vp, vp, vp, vp]),
+        "ksvd_refine_coefs": (st, [vp, vp, vp, i64, vp, vp, vp, vp]),
+        "ksvd_batched_omp": (st, [vp, vp, i32]),
+        "ksvd_graph_replays": (i64, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

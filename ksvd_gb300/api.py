@@ -58,7 +58,8 @@ class Handle:
     """One ksvd_handle: problem sizes, parameters, stream and device workspace."""
 
     def __init__(self, n, K, T, precision="fp32", mu_thresh=0.8, use_thresh=4,
-                 max_replace_signals=5000, seed=0x4B535644, stream=None, profile=False):
+                 max_replace_signals=5000, seed=0x4B535644, stream=None, profile=False,
+                 refine_final=False, graph=False):
         import torch
 
         self._lib = _native.load()
@@ -70,7 +71,9 @@ class Handle:
         p.use_thresh = int(use_thresh)
         p.max_replace_signals = int(max_replace_signals)
         p.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
-        p.flags = _native.FLAG_PROFILE if profile else 0
+        p.flags = ((_native.FLAG_PROFILE if profile else 0)
+                   | (_native.FLAG_REFINE_FINAL if refine_final else 0)
+                   | (_native.FLAG_GRAPH if graph else 0))
         self.params = p
         self.n, self.K, self.T = p.n, p.K, p.T
         if stream is None:
@@ -107,6 +110,10 @@ class Handle:
 
     def synchronize(self):
         self._check(self._lib.ksvd_synchronize(self._h))
+
+    def graph_replays(self) -> int:
+        """Iterations ksvd_iterate ran as CUDA-graph replays on this handle."""
+        return int(self._lib.ksvd_graph_replays(self._h))
 
     def stage_times(self, reset=False):
         """{stage: (milliseconds, calls)} accumulated while profiling (profile=True)."""
@@ -244,6 +251,70 @@ class Handle:
         self._check(self._lib.ksvd_iterate_host(self._h, vp(D), vp(X), N, int(iters), pp,
                                                 vp(idx), vp(coef), vp(nnz), vp(rmse)))
         return D, idx, coef, nnz, rmse[:iters]
+
+    def code_fixed(self, D, X, idx, nnz, save_chol=True):
+        """Least-squares coefficients on fixed supports; returns (coef, chol)."""
+        import torch
+
+        N = X.shape[0]
+        coef = torch.empty((N, self.T), dtype=torch.float32, device=X.device)
+        chol = (torch.empty((N, self.T * (self.T + 1) // 2), dtype=torch.float32,
+                            device=X.device) if save_chol else None)
+        self._check(self._lib.ksvd_code_fixed(self._h, _ptr(D), _ptr(X), N, _ptr(idx), _ptr(nnz),
+                                              _ptr(coef), _ptr(chol)))
+        return coef, chol
+
+    def refine_coefs(self, D, X, idx, nnz, coef, want_fp64=True):
+        """One FP64-residual refinement step of ``coef`` (in place); returns the FP64 values."""
+        import torch
+
+        N = X.shape[0]
+        c64 = (torch.empty((N, self.T), dtype=torch.float64, device=X.device)
+               if want_fp64 else None)
+        self._check(self._lib.ksvd_refine_coefs(self._h, _ptr(D), _ptr(X), N, _ptr(idx), _ptr(nnz),
+                                                _ptr(coef), _ptr(c64)))
+        return c64
+
+    def code_backward(self, D, X, idx, nnz, coef, chol, dcoef, dD=None, want_dX=True):
+        """Gradient through fixed-support coding: returns (dD, dX); dD accumulates."""
+        import torch
+
+        N = X.shape[0]
+        if dD is None:
+            dD = torch.zeros((self.K, self.n), dtype=torch.float32, device=X.device)
+        dX = torch.empty_like(X) if want_dX else None
+        self._check(self._lib.ksvd_code_backward(self._h, _ptr(D), _ptr(X), N, _ptr(idx),
+                                                 _ptr(nnz), _ptr(coef), _ptr(chol), _ptr(dcoef),
+                                                 _ptr(dD), _ptr(dX)))
+        return dD, dX
+
+    def batched_omp(self, problems):
+        """Batch-OMP of many independent problems in one persistent launch.
+
+        ``problems``: sequence of dicts with D (K, n) and X (N, n) float32 device tensors, T, and
+        optional eps2 (N,) float32 (error targets).  Returns [(idx, coef, nnz), ...]."""
+        import torch
+
+        arr = (_native.Problem * max(len(problems), 1))()
+        outs = []
+        for i, q in enumerate(problems):
+            D, X, T = q["D"], q["X"], int(q["T"])
+            K, n = D.shape
+            N = X.shape[0]
+            _need(D, "D", torch.float32, (K, n))
+            _need(X, "X", torch.float32, (N, n))
+            idx = torch.empty((N, T), dtype=torch.int32, device=X.device)
+            coef = torch.empty((N, T), dtype=torch.float32, device=X.device)
+            nnz = torch.empty((N,), dtype=torch.int32, device=X.device)
+            e = q.get("eps2")
+            if e is not None:
+                _need(e, "eps2", torch.float32, (N,))
+            arr[i] = _native.Problem(n, K, T, 0, N, D.data_ptr(), X.data_ptr(),
+                                     e.data_ptr() if e is not None else None, idx.data_ptr(),
+                                     coef.data_ptr(), nnz.data_ptr())
+            outs.append((idx, coef, nnz))
+        self._check(self._lib.ksvd_batched_omp(self._h, arr, len(problems)))
+        return outs
 
     def dense_gamma(self, idx, coef, nnz):
         import torch

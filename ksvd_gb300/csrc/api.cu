@@ -2,6 +2,7 @@
 // orchestration of the K-SVD iteration.  Replaces the reference's KSVD / OMP /
 // DictionaryUpdate classes (KSVD.cu, OMP.cu, DictionaryUpdate.cu), its enum-indexed
 // DeviceMemory pool (DeviceMemory.cu:19-138) and its cuBLAS handle base (CudaAlgorithm.cu).
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -44,6 +45,24 @@ struct ksvd_handle {
   double stage_ms[8] = {0};
   int64_t stage_calls[8] = {0};
   bool profiling() const { return (p.flags & KSVD_FLAG_PROFILE) != 0; }
+  // CUDA graph of one K-SVD iteration (KSVD_FLAG_GRAPH): captured on a side stream, replayed
+  struct GraphKey {
+    const void* p[12];
+    int64_t N;
+    bool operator==(const GraphKey& o) const {
+      for (int i = 0; i < 12; ++i) if (p[i] != o.p[i]) return false;
+      return N == o.N;
+    }
+  };
+  cudaStream_t gstream = nullptr;
+  cudaEvent_t gev[2] = {nullptr, nullptr};
+  cudaGraphExec_t gexec = nullptr;
+  GraphKey gkey{};
+  bool graph_broken = false;
+  int64_t graph_replays = 0;
+  // host copies of the batched call's tables (kept alive for the asynchronous uploads)
+  std::vector<ksvd::GemmDesc> batch_descs;
+  std::vector<ksvd::OmpJob> batch_jobs;
 };
 
 namespace {
@@ -52,7 +71,7 @@ enum BufId {
   B_DPAD, B_G, B_A0, B_XN2, B_LIST, B_START, B_BHIST, B_Y, B_GN2, B_C, B_AVEC, B_AD, B_PART,
   B_UNUSED, B_BITMAP, B_REPLACED, B_COUNTER, B_USE, B_BARRIER, B_ERR, B_PSUM, B_BVAL, B_BIDX,
   B_RMSE, B_M, B_MI, B_CLEARED, B_DEVERR, B_PERM, B_GPAD_IN, B_HX, B_HD, B_HIDX, B_HCOEF, B_HNNZ,
-  B_XHI, B_XLO, B_DHI, B_DLO, B_P, B_COUNT
+  B_XHI, B_XLO, B_DHI, B_DLO, B_P, B_BG, B_BA0, B_BDESC, B_BJOB, B_BQUEUE, B_ITER, B_COUNT
 };
 
 ksvd_status fail(ksvd_handle* h, ksvd_status s, const char* fmt, const char* detail = nullptr) {
@@ -302,10 +321,12 @@ ksvd_status update_ws(ksvd_handle* h, int64_t N, UpdateArgs& u) {
 }
 
 ksvd_status run_update(ksvd_handle* h, float* Dp, const float* X, int64_t N, const int32_t* idx,
-                       float* coef, const int32_t* nnz, const int32_t* perm_dev) {
+                       float* coef, const int32_t* nnz, const int32_t* perm_dev,
+                       const int* iter_ctr = nullptr) {
   UpdateArgs u;
   KSVD_TRY(update_ws(h, N, u));
   u.X = X; u.D = Dp; u.idx = idx; u.coef = coef; u.nnz = nnz; u.perm = perm_dev;
+  u.iter_ctr = iter_ctr;
   KSVD_TRY(gram_padded(h, Dp, u.G));          // the sweep maintains G = D'D from here on
   {
     StageScope sc(h, KSVD_STAGE_LISTS);
@@ -321,7 +342,7 @@ ksvd_status run_update(ksvd_handle* h, float* Dp, const float* X, int64_t N, con
 
 ksvd_status run_error(ksvd_handle* h, const float* Dp, const float* X, int64_t N,
                       const int32_t* idx, const float* coef, const int32_t* nnz,
-                      double* rmse_dev_slot) {
+                      double* rmse_dev_slot, const int* iter_ctr = nullptr) {
   ErrorArgs a;
   std::memset(&a, 0, sizeof(a));
   const int64_t nb = error_block_count(N);
@@ -335,6 +356,7 @@ ksvd_status run_error(ksvd_handle* h, const float* Dp, const float* X, int64_t N
   if (h->update_N == N) KSVD_TRY(ensure(h, B_BITMAP, (size_t)N, &bm));
   a.bitmap = bm;
   a.rmse_out = rmse_dev_slot;
+  a.iter_ctr = iter_ctr;
   StageScope sc(h, KSVD_STAGE_ERROR);
   KSVD_CK(h, launch_error(a, h->stream));
   h->error_N = N;
@@ -493,8 +515,17 @@ void ksvd_destroy(ksvd_handle* h) {
   for (auto& b : h->bufs)
     if (b.p) cudaFree(b.p);
   for (auto e : h->ev_pool) cudaEventDestroy(e);
+  if (h->gexec) cudaGraphExecDestroy(h->gexec);
+  if (h->gstream) {
+    cudaStreamSynchronize(h->gstream);
+    cudaStreamDestroy(h->gstream);
+  }
+  for (auto e : h->gev)
+    if (e) cudaEventDestroy(e);
   delete h;
 }
+
+int64_t ksvd_graph_replays(const ksvd_handle* h) { return h ? h->graph_replays : -1; }
 
 ksvd_status ksvd_read_stage_times(ksvd_handle* h, ksvd_stage_times* out, int32_t reset) {
   if (!h || !out) return KSVD_ERR_INVALID_ARGUMENT;
@@ -596,6 +627,80 @@ ksvd_status ksvd_omp(ksvd_handle* h, const float* D, const float* X, int64_t N, 
   return run_omp(h, G, A0, N, xn2, eps2, idx, coef, nnz);
 }
 
+// Many independent problems: one grouped GEMM launch for every G_p = D_p'D_p and alpha0_p =
+// D_p'X_p, then one persistent Batch-OMP launch whose warps pull signal chunks of all problems
+// from a device work queue.
+ksvd_status ksvd_batched_omp(ksvd_handle* h, const ksvd_problem* probs, int32_t nprob) {
+  if (!h || nprob < 0 || (nprob > 0 && !probs)) return KSVD_ERR_INVALID_ARGUMENT;
+  if (nprob == 0) return KSVD_OK;
+  int64_t g_off = 0, a_off = 0;
+  int tmax = 1;
+  std::vector<int64_t> goff(nprob), aoff(nprob);
+  for (int32_t i = 0; i < nprob; ++i) {
+    const ksvd_problem& q = probs[i];
+    if (q.n < 1 || q.n > kMaxN || q.K < 1 || q.K > kMaxK || q.T < 1 || q.T > kMaxT || q.T > q.K ||
+        q.N < 0)
+      return fail(h, KSVD_ERR_INVALID_ARGUMENT,
+                  "batched problem sizes out of range (1<=n<=1024, 1<=T<=min(K,64), K<=1024)%s");
+    if (q.N > 0 && (bad_ptr(q.D) || bad_ptr(q.X) || bad_ptr(q.idx) || bad_ptr(q.coef) ||
+                    bad_ptr(q.nnz)))
+      return fail(h, KSVD_ERR_INVALID_ARGUMENT, "batched problem with a null pointer%s");
+    if (q.N * q.T > 0x7fffffffLL)
+      return fail(h, KSVD_ERR_UNSUPPORTED, "N*T must stay below 2^31 per problem%s");
+    const int kp = omp_padded_k(q.K);
+    goff[i] = g_off;
+    aoff[i] = a_off;
+    g_off += round_up((int64_t)kp * kp, 64);
+    a_off += round_up((int64_t)kp * q.N, 64);
+    tmax = std::max(tmax, (int)q.T);
+  }
+  float *Gall = nullptr, *Aall = nullptr;
+  GemmDesc* ddev = nullptr;
+  OmpJob* jdev = nullptr;
+  unsigned long long* queue = nullptr;
+  int* de = nullptr;
+  KSVD_TRY(ensure(h, B_BG, (size_t)g_off, &Gall));
+  KSVD_TRY(ensure(h, B_BA0, (size_t)a_off, &Aall));
+  KSVD_TRY(ensure(h, B_BDESC, (size_t)2 * nprob, &ddev));
+  KSVD_TRY(ensure(h, B_BJOB, (size_t)nprob, &jdev));
+  KSVD_TRY(ensure(h, B_BQUEUE, 1, &queue));
+  KSVD_TRY(ensure(h, B_DEVERR, 1, &de));
+  auto& descs = h->batch_descs;
+  auto& jobs = h->batch_jobs;
+  descs.assign(2 * (size_t)nprob, GemmDesc{});
+  jobs.assign((size_t)nprob, OmpJob{});
+  int64_t tiles = 0, chunks = 0;
+  int nd = 0, nj = 0;
+  const int chunk = omp_batch_chunk();
+  for (int32_t i = 0; i < nprob; ++i) {
+    const ksvd_problem& q = probs[i];
+    if (q.N == 0) continue;
+    const int kp = omp_padded_k(q.K);
+    float* G = Gall + goff[i];
+    float* A0 = Aall + aoff[i];
+    tiles = gemm_desc_fill(descs[nd++], q.D, q.n, q.D, q.n, G, kp, q.K, kp, q.K, kp, q.n, tiles);
+    tiles = gemm_desc_fill(descs[nd++], q.D, q.n, q.X, q.n, A0, kp, q.K, kp, q.N, q.N, q.n, tiles);
+    OmpJob& j = jobs[nj++];
+    j.G = G; j.ldg = kp; j.A0 = A0; j.lda = kp; j.X = q.X; j.ldx = q.n; j.eps2 = q.eps2;
+    j.idx = q.idx; j.coef = q.coef; j.nnz = q.nnz; j.N = q.N; j.chunk_begin = chunks;
+    j.n = q.n; j.K = q.K; j.kpl = kp / 32; j.T = q.T;
+    chunks += (q.N + chunk - 1) / chunk;
+  }
+  if (nj == 0) return KSVD_OK;
+  // the host tables live in the handle, so the asynchronous copies read valid memory
+  KSVD_CK(h, cudaMemcpyAsync(ddev, descs.data(), sizeof(GemmDesc) * nd, cudaMemcpyHostToDevice,
+                             h->stream));
+  KSVD_CK(h, cudaMemcpyAsync(jdev, jobs.data(), sizeof(OmpJob) * nj, cudaMemcpyHostToDevice,
+                             h->stream));
+  {
+    StageScope sc(h, KSVD_STAGE_DTX);
+    KSVD_CK(h, launch_gemm_tn_f32_grouped(ddev, nd, tiles, h->stream));
+  }
+  StageScope sc(h, KSVD_STAGE_OMP);
+  KSVD_CK(h, launch_omp_batched(jdev, nj, chunks, tmax, queue, de, h->stream));
+  return KSVD_OK;
+}
+
 ksvd_status ksvd_update_dictionary(ksvd_handle* h, float* D, const float* X, int64_t N,
                                    const int32_t* idx, float* coef, const int32_t* nnz,
                                    const int32_t* perm) {
@@ -663,6 +768,95 @@ ksvd_status ksvd_clear_dict(ksvd_handle* h, float* D, const float* X, int64_t N,
   return KSVD_OK;
 }
 
+namespace {
+
+// One K-SVD iteration (S/KSVD.cu:55-131 loop body) on the handle's stream.  The permutation and
+// the RMSE slot are indexed by the device iteration counter, which the iteration advances last,
+// so the same launches serve every iteration and a captured graph can be replayed.
+ksvd_status iteration_body(ksvd_handle* h, float* Dp, float* G, float* A0, const float* X,
+                           int64_t N, int32_t* idx, float* coef, int32_t* nnz,
+                           const int32_t* pd, double* rd, int32_t* cd, int* ctr) {
+  KSVD_TRY(dtx_padded(h, Dp, X, N, A0));                             // OMP.cu:44
+  KSVD_TRY(run_omp(h, G, A0, N, nullptr, nullptr, idx, coef, nnz));  // OMP.cu:55
+  KSVD_TRY(run_update(h, Dp, X, N, idx, coef, nnz, pd, ctr));       // KSVD.cu:97-114
+  KSVD_TRY(run_error(h, Dp, X, N, idx, coef, nnz, rd, ctr));        // KSVD.cu:119
+  KSVD_TRY(gram_padded(h, Dp, G));                                   // G of the updated D
+  KSVD_TRY(run_clear(h, Dp, G, X, N, cd));                           // KSVD.cu:126
+  KSVD_CK(h, launch_advance_counter(ctr, h->stream));
+  return KSVD_OK;
+}
+
+// Runs the calls in between on the handle's private non-blocking stream, fenced to the
+// caller's stream on entry and on exit (stream capture is not allowed on the legacy stream).
+struct SideStream {
+  ksvd_handle* h;
+  cudaStream_t user = nullptr;
+  bool active = false;
+  explicit SideStream(ksvd_handle* hh) : h(hh) {}
+  ksvd_status enter() {
+    if (!h->gstream) {
+      KSVD_CK(h, cudaStreamCreateWithFlags(&h->gstream, cudaStreamNonBlocking));
+      for (auto& e : h->gev) KSVD_CK(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    user = h->stream;
+    KSVD_CK(h, cudaEventRecord(h->gev[0], user));
+    KSVD_CK(h, cudaStreamWaitEvent(h->gstream, h->gev[0], 0));
+    h->stream = h->gstream;
+    active = true;
+    return KSVD_OK;
+  }
+  ~SideStream() {
+    if (!active) return;
+    cudaEventRecord(h->gev[1], h->gstream);
+    cudaStreamWaitEvent(user, h->gev[1], 0);
+    h->stream = user;
+  }
+};
+
+// Replays `count` iterations from a graph of iteration_body, capturing it first when the cached
+// graph was made for other buffers.  Returns false (nothing launched) when capture is refused.
+bool replay_graph(ksvd_handle* h, const ksvd_handle::GraphKey& key, int32_t count, float* Dp,
+                  float* G, float* A0, const float* X, int64_t N, int32_t* idx, float* coef,
+                  int32_t* nnz, const int32_t* pd, double* rd, int32_t* cd, int* ctr) {
+  if (h->graph_broken) return false;
+  if (!h->gexec || !(h->gkey == key)) {
+    if (h->gexec) {
+      cudaGraphExecDestroy(h->gexec);
+      h->gexec = nullptr;
+    }
+    if (cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      h->graph_broken = true;
+      return false;
+    }
+    const ksvd_status st = iteration_body(h, Dp, G, A0, X, N, idx, coef, nnz, pd, rd, cd, ctr);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
+    cudaGraphExec_t ex = nullptr;
+    const bool ok = st == KSVD_OK && ec == cudaSuccess && g &&
+                    cudaGraphInstantiate(&ex, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    if (!ok) {
+      if (ex) cudaGraphExecDestroy(ex);
+      h->graph_broken = true;
+      h->err.clear();
+      return false;
+    }
+    h->gexec = ex;
+    h->gkey = key;
+  }
+  for (int32_t r = 0; r < count; ++r)
+    if (cudaGraphLaunch(h->gexec, h->stream) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+  h->graph_replays += count;
+  return true;
+}
+
+}  // namespace
+
 ksvd_status ksvd_iterate(ksvd_handle* h, float* D, const float* X, int64_t N, int32_t iters,
                          const int32_t* perms, int32_t* idx, float* coef, int32_t* nnz,
                          double* rmse) {
@@ -673,25 +867,45 @@ ksvd_status ksvd_iterate(ksvd_handle* h, float* D, const float* X, int64_t N, in
   if ((int64_t)N * h->p.T > 0x7fffffffLL)
     return fail(h, KSVD_ERR_UNSUPPORTED, "N*T must stay below 2^31%s");
   const int Kp = h->Kp;
+  const bool graph = (h->p.flags & KSVD_FLAG_GRAPH) && !h->profiling() && iters > 1;
+  SideStream side(h);
+  if (graph) KSVD_TRY(side.enter());
   drop_xsplit(h);
   float *Dp = nullptr, *G = nullptr, *A0 = nullptr;
   double* rd = nullptr;
   int32_t *pd = nullptr, *cd = nullptr;
+  int* ctr = nullptr;
   KSVD_TRY(load_dict(h, D, &Dp));
   KSVD_TRY(ensure(h, B_G, (size_t)Kp * Kp, &G));
   KSVD_TRY(ensure(h, B_A0, (size_t)Kp * N, &A0));
   KSVD_TRY(ensure(h, B_RMSE, 1024, &rd));
   KSVD_TRY(ensure(h, B_CLEARED, 1, &cd));
+  KSVD_TRY(ensure(h, B_ITER, 1, &ctr));
+  KSVD_CK(h, cudaMemsetAsync(ctr, 0, sizeof(int), h->stream));
   if (iters > 0) KSVD_TRY(upload_perm(h, perms, iters, &pd));
   KSVD_CK(h, launch_normcols(Dp, h->p.n, h->p.K, h->stream));         // KSVD.cu:57
   KSVD_TRY(gram_padded(h, Dp, G));                                     // KSVD.cu:64
-  for (int32_t it = 0; it < iters; ++it) {
-    KSVD_TRY(dtx_padded(h, Dp, X, N, A0));                             // OMP.cu:44
-    KSVD_TRY(run_omp(h, G, A0, N, nullptr, nullptr, idx, coef, nnz));  // OMP.cu:55
-    KSVD_TRY(run_update(h, Dp, X, N, idx, coef, nnz, pd + (size_t)it * h->p.K));  // KSVD.cu:97-114
-    KSVD_TRY(run_error(h, Dp, X, N, idx, coef, nnz, rd + it));        // KSVD.cu:119
-    KSVD_TRY(gram_padded(h, Dp, G));                                   // G of the updated D
-    KSVD_TRY(run_clear(h, Dp, G, X, N, cd));                           // KSVD.cu:126
+  int32_t done = 0;
+  if (iters > 0) {
+    // the first iteration runs eagerly: it sizes every workspace buffer (no allocation may
+    // happen under capture) and makes the mixed path's BF16 copy of X for this call
+    KSVD_TRY(iteration_body(h, Dp, G, A0, X, N, idx, coef, nnz, pd, rd, cd, ctr));
+    done = 1;
+  }
+  if (graph && done < iters) {
+    ksvd_handle::GraphKey key{{Dp, G, A0, X, idx, coef, nnz, pd, rd, cd, ctr,
+                               reinterpret_cast<const void*>((intptr_t)h->p.precision)},
+                              N};
+    if (replay_graph(h, key, iters - done, Dp, G, A0, X, N, idx, coef, nnz, pd, rd, cd, ctr))
+      done = iters;
+  }
+  for (; done < iters; ++done)
+    KSVD_TRY(iteration_body(h, Dp, G, A0, X, N, idx, coef, nnz, pd, rd, cd, ctr));
+  if (iters > 0 && (h->p.flags & KSVD_FLAG_REFINE_FINAL)) {
+    int* de = nullptr;
+    KSVD_TRY(ensure(h, B_DEVERR, 1, &de));
+    KSVD_CK(h, launch_refine(Dp, h->p.n, h->p.K, G, Kp, X, N, h->p.T, idx, nnz, coef, nullptr, de,
+                             h->stream));                            // G is D'D after clearDict
   }
   drop_xsplit(h);
   KSVD_TRY(store_dict(h, Dp, D));
@@ -724,6 +938,50 @@ ksvd_status ksvd_iterate_host(ksvd_handle* h, float* D, const float* X, int64_t 
   KSVD_CK(h, cudaMemcpyAsync(coef, dC, sizeof(float) * (size_t)N * T, cudaMemcpyDeviceToHost, h->stream));
   KSVD_CK(h, cudaMemcpyAsync(nnz, dN, sizeof(int32_t) * (size_t)N, cudaMemcpyDeviceToHost, h->stream));
   KSVD_CK(h, cudaStreamSynchronize(h->stream));
+  return KSVD_OK;
+}
+
+ksvd_status ksvd_code_fixed(ksvd_handle* h, const float* D, const float* X, int64_t N,
+                            const int32_t* idx, const int32_t* nnz, float* coef, float* chol) {
+  if (!h || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(nnz) || bad_ptr(coef) || N < 0)
+    return KSVD_ERR_INVALID_ARGUMENT;
+  if (N == 0) return KSVD_OK;
+  float *Dp = nullptr, *G = nullptr;
+  int* de = nullptr;
+  KSVD_TRY(ensure(h, B_DEVERR, 1, &de));
+  KSVD_TRY(load_dict(h, D, &Dp));
+  KSVD_TRY(ensure(h, B_G, (size_t)h->Kp * h->Kp, &G));
+  KSVD_TRY(gram_padded(h, Dp, G));
+  KSVD_CK(h, launch_code_fixed(D, h->p.n, h->p.K, G, h->Kp, X, N, h->p.T, idx, nnz, coef, chol,
+                               de, h->stream));
+  return KSVD_OK;
+}
+
+ksvd_status ksvd_refine_coefs(ksvd_handle* h, const float* D, const float* X, int64_t N,
+                              const int32_t* idx, const int32_t* nnz, float* coef, double* coef64) {
+  if (!h || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(nnz) || bad_ptr(coef) || N < 0)
+    return KSVD_ERR_INVALID_ARGUMENT;
+  if (N == 0) return KSVD_OK;
+  float *Dp = nullptr, *G = nullptr;
+  int* de = nullptr;
+  KSVD_TRY(ensure(h, B_DEVERR, 1, &de));
+  KSVD_TRY(load_dict(h, D, &Dp));
+  KSVD_TRY(ensure(h, B_G, (size_t)h->Kp * h->Kp, &G));
+  KSVD_TRY(gram_padded(h, Dp, G));
+  KSVD_CK(h, launch_refine(D, h->p.n, h->p.K, G, h->Kp, X, N, h->p.T, idx, nnz, coef, coef64,
+                           de, h->stream));
+  return KSVD_OK;
+}
+
+ksvd_status ksvd_code_backward(ksvd_handle* h, const float* D, const float* X, int64_t N,
+                               const int32_t* idx, const int32_t* nnz, const float* coef,
+                               const float* chol, const float* dcoef, float* dD, float* dX) {
+  if (!h || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(nnz) || bad_ptr(coef) ||
+      bad_ptr(chol) || bad_ptr(dcoef) || N < 0)
+    return KSVD_ERR_INVALID_ARGUMENT;
+  if (N == 0) return KSVD_OK;
+  KSVD_CK(h, launch_code_backward(D, h->p.n, h->p.K, X, N, h->p.T, idx, nnz, coef, chol, dcoef,
+                                  dD, dX, h->stream));
   return KSVD_OK;
 }
 

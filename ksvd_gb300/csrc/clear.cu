@@ -79,7 +79,7 @@ error_kernel(ErrorArgs A) {
 }
 
 __global__ void rmse_kernel(const double* __restrict__ part, int64_t nb, double denom,
-                            double* __restrict__ out) {
+                            double* __restrict__ out, const int* __restrict__ iter_ctr) {
   __shared__ double red[32];
   double t = 0.0;
   for (int64_t i = threadIdx.x; i < nb; i += blockDim.x) t += part[i];
@@ -90,7 +90,7 @@ __global__ void rmse_kernel(const double* __restrict__ part, int64_t nb, double 
   if (w == 0) {
     t = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
     t = warp_sum_d(t);
-    if (lane == 0) *out = sqrt(t / denom);
+    if (lane == 0) out[iter_ctr ? *iter_ctr : 0] = sqrt(t / denom);
   }
 }
 
@@ -238,7 +238,8 @@ cudaError_t launch_error(const ErrorArgs& a, cudaStream_t st) {
   else error_kernel<32><<<(unsigned)nb, kErrWarps * 32, 0, st>>>(a);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  rmse_kernel<<<1, 1024, 0, st>>>(a.part_sum, nb, (double)a.n * (double)a.N, a.rmse_out);
+  rmse_kernel<<<1, 1024, 0, st>>>(a.part_sum, nb, (double)a.n * (double)a.N, a.rmse_out,
+                                  a.iter_ctr);
   return cudaGetLastError();
 }
 

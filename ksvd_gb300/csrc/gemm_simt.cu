@@ -15,16 +15,15 @@ namespace {
 
 constexpr int BM = 128, BN = 128, BK = 8, NT = 256;
 
-__global__ void __launch_bounds__(NT, 2)
-gemm_tn_f32_kernel(const float* __restrict__ A, int64_t lda, const float* __restrict__ B,
-                   int64_t ldb, float* __restrict__ C, int64_t ldc, int M, int Mst, int64_t Ncols,
-                   int64_t Nst, int inner, bool vec_a, bool vec_b, bool vec_c) {
-  __shared__ __align__(16) float As[2][BK][BM];
-  __shared__ __align__(16) float Bs[2][BK][BN];
+// One 128 x 128 output tile at (m0 atoms, n0 signals).
+__device__ __forceinline__ void gemm_tile(const float* __restrict__ A, int64_t lda,
+                                          const float* __restrict__ B, int64_t ldb,
+                                          float* __restrict__ C, int64_t ldc, int M, int Mst,
+                                          int64_t Ncols, int64_t Nst, int inner, bool vec_a,
+                                          bool vec_b, bool vec_c, int64_t m0, int64_t n0,
+                                          float (&As)[2][BK][BM], float (&Bs)[2][BK][BN]) {
   const int tid = threadIdx.x;
   const int ty = tid & 15, tx = tid >> 4;
-  const int64_t m0 = (int64_t)blockIdx.y * BM;
-  const int64_t n0 = (int64_t)blockIdx.x * BN;
 
   // loader coordinates: row (atom or signal) and 4-wide inner offset
   const int lrow = tid >> 1, lc4 = (tid & 1) * 4;
@@ -111,6 +110,36 @@ gemm_tn_f32_kernel(const float* __restrict__ A, int64_t lda, const float* __rest
   }
 }
 
+__global__ void __launch_bounds__(NT, 2)
+gemm_tn_f32_kernel(const float* __restrict__ A, int64_t lda, const float* __restrict__ B,
+                   int64_t ldb, float* __restrict__ C, int64_t ldc, int M, int Mst, int64_t Ncols,
+                   int64_t Nst, int inner, bool vec_a, bool vec_b, bool vec_c) {
+  __shared__ __align__(16) float As[2][BK][BM];
+  __shared__ __align__(16) float Bs[2][BK][BN];
+  gemm_tile(A, lda, B, ldb, C, ldc, M, Mst, Ncols, Nst, inner, vec_a, vec_b, vec_c,
+            (int64_t)blockIdx.y * BM, (int64_t)blockIdx.x * BN, As, Bs);
+}
+
+// Many independent products in one launch: block b works on the tile of the problem whose tile
+// range [tile_begin, tile_begin + tiles_m * tiles_n) holds b (binary search over the table).
+__global__ void __launch_bounds__(NT, 2)
+gemm_tn_f32_grouped_kernel(const GemmDesc* __restrict__ descs, int ndesc) {
+  __shared__ __align__(16) float As[2][BK][BM];
+  __shared__ __align__(16) float Bs[2][BK][BN];
+  const int64_t b = blockIdx.x;
+  int lo = 0, hi = ndesc - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (descs[mid].tile_begin <= b) lo = mid; else hi = mid - 1;
+  }
+  const GemmDesc& d = descs[lo];
+  const int64_t t = b - d.tile_begin;
+  if (t >= (int64_t)d.tiles_m * d.tiles_n) return;
+  gemm_tile(d.A, d.lda, d.B, d.ldb, d.C, d.ldc, d.M_load, d.M_store, d.N_load, d.N_store,
+            d.inner, d.vec_a, d.vec_b, d.vec_c, (t % d.tiles_m) * BM, (t / d.tiles_m) * BN, As,
+            Bs);
+}
+
 inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
 }  // namespace
@@ -129,6 +158,29 @@ cudaError_t launch_gemm_tn_f32(const float* A, int64_t lda, const float* B, int6
   dim3 grid((unsigned)gx, (unsigned)gy);
   gemm_tn_f32_kernel<<<grid, NT, 0, st>>>(A, lda, B, ldb, C, ldc, M_load, M_store, N_load,
                                           N_store, inner, va, vb, vc);
+  return cudaGetLastError();
+}
+
+int64_t gemm_desc_fill(GemmDesc& d, const float* A, int64_t lda, const float* B, int64_t ldb,
+                       float* C, int64_t ldc, int M_load, int M_store, int64_t N_load,
+                       int64_t N_store, int inner, int64_t tile_begin) {
+  d.A = A; d.lda = lda; d.B = B; d.ldb = ldb; d.C = C; d.ldc = ldc;
+  d.M_load = M_load; d.M_store = M_store; d.N_load = N_load; d.N_store = N_store;
+  d.inner = inner;
+  d.vec_a = (lda % 4 == 0) && aligned16(A);
+  d.vec_b = (ldb % 4 == 0) && aligned16(B);
+  d.vec_c = (ldc % 4 == 0) && aligned16(C);
+  d.tiles_m = (int)((M_store + BM - 1) / BM);
+  d.tiles_n = (N_store + BN - 1) / BN;
+  d.tile_begin = tile_begin;
+  return tile_begin + (int64_t)d.tiles_m * d.tiles_n;
+}
+
+cudaError_t launch_gemm_tn_f32_grouped(const GemmDesc* descs_dev, int ndesc, int64_t total_tiles,
+                                       cudaStream_t st) {
+  if (ndesc <= 0 || total_tiles <= 0) return cudaSuccess;
+  if (total_tiles > 0x7fffffffLL) return cudaErrorInvalidValue;
+  gemm_tn_f32_grouped_kernel<<<(unsigned)total_tiles, NT, 0, st>>>(descs_dev, ndesc);
   return cudaGetLastError();
 }
 

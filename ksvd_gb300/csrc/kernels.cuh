@@ -62,7 +62,8 @@ struct UpdateArgs {
   const int32_t* idx;    // N x T
   float* coef;           // N x T (updated in place)
   const int32_t* nnz;    // N
-  const int32_t* perm;   // K
+  const int32_t* perm;   // K (or iters x K with iter_ctr)
+  const int* iter_ctr;   // nullable: use perm + (*iter_ctr) * K (graph replays)
   int max_signals;
   // workspace
   int32_t* list;         // total entries (signal*T + slot), per-atom ascending signal order
@@ -103,7 +104,8 @@ struct ErrorArgs {
   double* part_sum;      // per error block
   float* bucket_val;     // per error block: max masked error
   int64_t* bucket_idx;   // per error block: its signal (lowest on ties)
-  double* rmse_out;      // device scalar
+  double* rmse_out;      // device scalar (rmse_out[*iter_ctr] when iter_ctr is set)
+  const int* iter_ctr;   // nullable
 };
 int64_t error_block_count(int64_t N);
 cudaError_t launch_error(const ErrorArgs& a, cudaStream_t st);
@@ -126,5 +128,57 @@ struct ClearArgs {
 };
 // m, mi: Kp scratch floats / ints (per-column largest off-diagonal G^2 and its row)
 cudaError_t launch_clear_dict(const ClearArgs& a, float* m, int* mi, cudaStream_t st);
+
+// *ctr += 1 (one thread): the iteration counter that graph-replayed iterations index by.
+cudaError_t launch_advance_counter(int* ctr, cudaStream_t st);
+
+// ---- batched Batch-OMP: many problems in one persistent launch (omp.cu) ---------------------------
+struct OmpJob {
+  const float* G; int64_t ldg;      // Kp x Kp Gram (rows >= K zero)
+  const float* A0; int64_t lda;     // Kp x N alpha0 (rows >= K zero)
+  const float* X; int64_t ldx;      // n x N signals (read for ||x||^2 in error mode)
+  const float* eps2;                // N error targets, or null (T-sparse)
+  int32_t* idx; float* coef; int32_t* nnz;   // N x T slots, N
+  int64_t N; int64_t chunk_begin;   // first work-queue chunk of this job
+  int n, K, kpl, T;                 // kpl = Kp / 32 (4, 8, 16 or 32)
+};
+int omp_batch_chunk();              // signals per work-queue chunk
+// jobs_dev sorted by chunk_begin; tmax = max T over the jobs.  Zeroes *queue on the stream.
+cudaError_t launch_omp_batched(const OmpJob* jobs_dev, int njobs, int64_t total_chunks, int tmax,
+                               unsigned long long* queue, int* dev_err, cudaStream_t st);
+
+// ---- grouped FP32 GEMM: many C = A'B products (different sizes) in one launch -------------------
+struct GemmDesc {
+  const float* A; int64_t lda;
+  const float* B; int64_t ldb;
+  float* C; int64_t ldc;
+  int M_load, M_store; int64_t N_load, N_store;
+  int inner;
+  int tiles_m; int64_t tiles_n; int64_t tile_begin;
+  bool vec_a, vec_b, vec_c;
+};
+// Fills d (same meaning of the sizes as launch_gemm_tn_f32); returns tile_begin + its tiles.
+int64_t gemm_desc_fill(GemmDesc& d, const float* A, int64_t lda, const float* B, int64_t ldb,
+                       float* C, int64_t ldc, int M_load, int M_store, int64_t N_load,
+                       int64_t N_store, int inner, int64_t tile_begin);
+// descs_dev: device copy of the table, sorted by tile_begin (as gemm_desc_fill chains them).
+cudaError_t launch_gemm_tn_f32_grouped(const GemmDesc* descs_dev, int ndesc, int64_t total_tiles,
+                                       cudaStream_t st);
+
+// ---- fixed-support coding and its adjoint (adjoint.cu) ---------------------------------------
+// G: D'D with leading dimension ldg (>= K).  chol: N x T(T+1)/2 packed lower factors.
+cudaError_t launch_code_fixed(const float* D, int n, int K, const float* G, int ldg,
+                              const float* X, int64_t N, int T, const int32_t* idx,
+                              const int32_t* nnz, float* coef, float* chol, int* dev_err,
+                              cudaStream_t st);
+// One FP64-residual refinement step of the coefficients on fixed supports (coef in place).
+cudaError_t launch_refine(const float* D, int n, int K, const float* G, int ldg, const float* X,
+                          int64_t N, int T, const int32_t* idx, const int32_t* nnz, float* coef,
+                          double* coef64, int* dev_err, cudaStream_t st);
+// dD (n x K, accumulated: zero it first) and dX (n x N, written); either may be null.
+cudaError_t launch_code_backward(const float* D, int n, int K, const float* X, int64_t N, int T,
+                                 const int32_t* idx, const int32_t* nnz, const float* coef,
+                                 const float* chol, const float* dcoef, float* dD, float* dX,
+                                 cudaStream_t st);
 
 }  // namespace ksvd

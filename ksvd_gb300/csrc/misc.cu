@@ -87,6 +87,13 @@ cudaError_t launch_copy_pad_cols(const float* src, int n, int K, float* dst, int
   return cudaGetLastError();
 }
 
+__global__ void advance_counter_kernel(int* c) { *c += 1; }
+
+cudaError_t launch_advance_counter(int* ctr, cudaStream_t st) {
+  advance_counter_kernel<<<1, 1, 0, st>>>(ctr);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_col_norm2(const float* X, int n, int64_t N, float* out, cudaStream_t st) {
   if (N <= 0) return cudaSuccess;
   col_norm2_kernel<<<(unsigned)((N + 7) / 8), 256, 0, st>>>(X, n, N, out);

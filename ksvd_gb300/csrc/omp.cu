@@ -38,26 +38,23 @@ __device__ __forceinline__ void put(V (&a)[SPL], int j, V v) {
   else { if (j == 0) a[0] = v; else a[1] = v; }
 }
 
+// Batch-OMP of one signal by one warp.  a0p: the signal's alpha0 column (Kp = 32*KPL rows, rows
+// >= K zero); L: (TMAX x TMAX+1) and a0s: (32*KPL) floats of this warp's shared memory.  emode:
+// stop once ||x||^2 - ||y||^2 <= e2 (xn2 = ||x||^2).  Writes T slots of idx/coef and nnz.
 template <int KPL, int TMAX>
-__global__ void __launch_bounds__(kOmpWarps * 32, (TMAX <= 32 ? 3 : 1))
-omp_kernel(const float* __restrict__ G, int64_t ldg, const float* __restrict__ A0, int64_t lda,
-           int K, int64_t N, int T, const float* __restrict__ xnorm2,
-           const float* __restrict__ eps2, int32_t* __restrict__ idx_out,
-           float* __restrict__ coef_out, int32_t* __restrict__ nnz_out, int* __restrict__ dev_err) {
+__device__ __forceinline__ void omp_signal(const float* __restrict__ G, int64_t ldg,
+                                           const float* __restrict__ a0col, int K, int T,
+                                           bool emode, float e2, float xn2,
+                                           int32_t* __restrict__ idx_s, float* __restrict__ coef_s,
+                                           int32_t* __restrict__ nnz_s, float* L, float* a0s,
+                                           bool& numeric_bad) {
   constexpr int M4 = KPL / 4;    // float4 groups per lane; lane owns rows 128*m + 4*lane + q
   constexpr int SPL = TMAX / 32; // support slots per lane; lane owns slots lane + 32*j
   constexpr int LS = TMAX + 1;   // row stride of L in shared memory
-  extern __shared__ __align__(16) float smem[];
   const int lane = threadIdx.x & 31;
-  const int wib = threadIdx.x >> 5;
-  float* L = smem + (size_t)wib * (TMAX * LS + 32 * KPL);   // Cholesky factor, (TMAX x LS)
-  float* a0s = L + TMAX * LS;                                // this warp's alpha0 column
-  const int64_t warps_total = (int64_t)gridDim.x * kOmpWarps;
-  bool numeric_bad = false;
-
-  for (int64_t s = (int64_t)blockIdx.x * kOmpWarps + wib; s < N; s += warps_total) {
+  {
     float al[M4][4];
-    const float* a0p = A0 + s * lda + 4 * lane;
+    const float* a0p = a0col + 4 * lane;
     __syncwarp();                      // the previous signal's last reads of a0s are done
 #pragma unroll
     for (int m = 0; m < M4; ++m) {
@@ -71,9 +68,6 @@ omp_kernel(const float* __restrict__ G, int64_t ldg, const float* __restrict__ A
 #pragma unroll
     for (int j = 0; j < SPL; ++j) { ind[j] = -1; y[j] = 0.f; c[j] = 0.f; }
 
-    const bool emode = eps2 != nullptr;
-    const float e2 = emode ? eps2[s] : 0.f;
-    const float xn2 = emode ? xnorm2[s] : 0.f;
     float r2 = xn2;
     int i = 0;
     while (i < T) {
@@ -207,12 +201,99 @@ omp_kernel(const float* __restrict__ G, int64_t ldg, const float* __restrict__ A
       const int q = lane + 32 * j;
       if (q < T) {
         const bool used = q < i;
-        idx_out[s * T + q] = used ? ind[j] : -1;
-        coef_out[s * T + q] = used ? c[j] : 0.f;
+        idx_s[q] = used ? ind[j] : -1;
+        coef_s[q] = used ? c[j] : 0.f;
         if (used && !finitef(c[j])) numeric_bad = true;
       }
     }
-    if (lane == 0) nnz_out[s] = i;
+    if (lane == 0) *nnz_s = i;
+  }
+}
+
+template <int KPL, int TMAX>
+__global__ void __launch_bounds__(kOmpWarps * 32, (TMAX <= 32 ? 3 : 1))
+omp_kernel(const float* __restrict__ G, int64_t ldg, const float* __restrict__ A0, int64_t lda,
+           int K, int64_t N, int T, const float* __restrict__ xnorm2,
+           const float* __restrict__ eps2, int32_t* __restrict__ idx_out,
+           float* __restrict__ coef_out, int32_t* __restrict__ nnz_out, int* __restrict__ dev_err) {
+  constexpr int LS = TMAX + 1;
+  extern __shared__ __align__(16) float smem[];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  float* L = smem + (size_t)wib * (TMAX * LS + 32 * KPL);   // Cholesky factor, (TMAX x LS)
+  float* a0s = L + TMAX * LS;                                // this warp's alpha0 column
+  const int64_t warps_total = (int64_t)gridDim.x * kOmpWarps;
+  bool numeric_bad = false;
+  const bool emode = eps2 != nullptr;
+  for (int64_t s = (int64_t)blockIdx.x * kOmpWarps + wib; s < N; s += warps_total)
+    omp_signal<KPL, TMAX>(G, ldg, A0 + s * lda, K, T, emode, emode ? eps2[s] : 0.f,
+                          emode ? xnorm2[s] : 0.f, idx_out + s * T, coef_out + s * T,
+                          nnz_out + s, L, a0s, numeric_bad);
+  if (__any_sync(KSVD_FULL_MASK, numeric_bad) && lane == 0) atomicOr(dev_err, kDevErrNumeric);
+}
+
+// Many independent Batch-OMP problems (different K, T, N; T-sparse or error-constrained) in one
+// persistent launch.  Work queue: each warp takes the next chunk of kChunk signals with one
+// atomicAdd on *queue (zeroed before the launch); chunk c belongs to the job whose range
+// [chunk_begin, chunk_begin + ceil(N / kChunk)) holds it.  In error-constrained jobs ||x||^2
+// comes from X in the same pass.
+constexpr int kBatchChunk = 16;
+
+template <int TMAX>
+__global__ void __launch_bounds__(kOmpWarps * 32, (TMAX <= 32 ? 2 : 1))
+omp_batched_kernel(const OmpJob* __restrict__ jobs, int njobs, int64_t total_chunks,
+                   unsigned long long* __restrict__ queue, int* __restrict__ dev_err) {
+  constexpr int LS = TMAX + 1;
+  extern __shared__ __align__(16) float smem[];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  float* L = smem + (size_t)wib * (TMAX * LS + 32 * 32);
+  float* a0s = L + TMAX * LS;
+  bool numeric_bad = false;
+  for (;;) {
+    unsigned long long c = 0;
+    if (lane == 0) c = atomicAdd(queue, 1ull);
+    c = __shfl_sync(KSVD_FULL_MASK, c, 0);
+    if ((int64_t)c >= total_chunks) break;
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (jobs[mid].chunk_begin <= (int64_t)c) lo = mid; else hi = mid - 1;
+    }
+    const OmpJob& jb = jobs[lo];
+    const int64_t s0 = ((int64_t)c - jb.chunk_begin) * kBatchChunk;
+    const int64_t s1 = min(jb.N, s0 + kBatchChunk);
+    const bool emode = jb.eps2 != nullptr;
+    for (int64_t s = s0; s < s1; ++s) {
+      float xn2 = 0.f, e2 = 0.f;
+      if (emode) {
+        const float* x = jb.X + s * jb.ldx;
+        for (int r = lane; r < jb.n; r += 32) xn2 = fmaf(x[r], x[r], xn2);
+        xn2 = warp_sum(xn2);
+        e2 = jb.eps2[s];
+      }
+      const float* a0 = jb.A0 + s * jb.lda;
+      int32_t* io = jb.idx + s * jb.T;
+      float* co = jb.coef + s * jb.T;
+      switch (jb.kpl) {
+        case 4:
+          omp_signal<4, TMAX>(jb.G, jb.ldg, a0, jb.K, jb.T, emode, e2, xn2, io, co, jb.nnz + s, L,
+                              a0s, numeric_bad);
+          break;
+        case 8:
+          omp_signal<8, TMAX>(jb.G, jb.ldg, a0, jb.K, jb.T, emode, e2, xn2, io, co, jb.nnz + s, L,
+                              a0s, numeric_bad);
+          break;
+        case 16:
+          omp_signal<16, TMAX>(jb.G, jb.ldg, a0, jb.K, jb.T, emode, e2, xn2, io, co, jb.nnz + s,
+                               L, a0s, numeric_bad);
+          break;
+        default:
+          omp_signal<32, TMAX>(jb.G, jb.ldg, a0, jb.K, jb.T, emode, e2, xn2, io, co, jb.nnz + s,
+                               L, a0s, numeric_bad);
+          break;
+      }
+    }
   }
   if (__any_sync(KSVD_FULL_MASK, numeric_bad) && lane == 0) atomicOr(dev_err, kDevErrNumeric);
 }
@@ -239,7 +320,39 @@ cudaError_t launch_omp_t(const float* G, int64_t ldg, const float* A0, int64_t l
   return cudaGetLastError();
 }
 
+template <int TMAX>
+cudaError_t launch_omp_batched_t(const OmpJob* jobs, int njobs, int64_t total_chunks,
+                                 unsigned long long* queue, int* dev_err, cudaStream_t st) {
+  const size_t smem = (size_t)kOmpWarps * (TMAX * (TMAX + 1) + 32 * 32) * sizeof(float);
+  auto kern = omp_batched_kernel<TMAX>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kOmpWarps * 32, smem);
+  if (per_sm < 1) per_sm = 1;
+  const int64_t need = (total_chunks + kOmpWarps - 1) / kOmpWarps;
+  int64_t blocks = (int64_t)sms * per_sm;
+  if (blocks > need) blocks = need;
+  e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return e;
+  kern<<<(unsigned)blocks, kOmpWarps * 32, smem, st>>>(jobs, njobs, total_chunks, queue, dev_err);
+  return cudaGetLastError();
+}
+
 }  // namespace
+
+int omp_batch_chunk() { return kBatchChunk; }
+
+cudaError_t launch_omp_batched(const OmpJob* jobs_dev, int njobs, int64_t total_chunks, int tmax,
+                               unsigned long long* queue, int* dev_err, cudaStream_t st) {
+  if (njobs <= 0 || total_chunks <= 0) return cudaSuccess;
+  if (tmax < 1 || tmax > kMaxT) return cudaErrorInvalidValue;
+  if (tmax <= 32) return launch_omp_batched_t<32>(jobs_dev, njobs, total_chunks, queue, dev_err, st);
+  return launch_omp_batched_t<64>(jobs_dev, njobs, total_chunks, queue, dev_err, st);
+}
 
 int omp_padded_k(int K) {
   return K <= 128 ? 128 : K <= 256 ? 256 : K <= 512 ? 512 : 1024;

@@ -308,6 +308,7 @@ struct SweepArgs {
   float* coef;
   const int32_t* nnz;
   const int32_t* perm;
+  const int* iter_ctr;
   int max_signals;
   const int32_t* list;
   const int64_t* start;
@@ -672,10 +673,11 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
   Sweep<NPL> S(A, sm, red_f, red_i, &sflag);
   const int K = A.K, n = A.n, tid = threadIdx.x;
   constexpr int HALF = Sweep<NPL>::HALF;
+  const int32_t* perm = A.perm + (A.iter_ctr ? (int64_t)(*A.iter_ctr) * K : 0);
   // every CTA checks the whole permutation itself, so all of them leave together or none does
   int bad = 0;
   for (int k = tid; k < K; k += blockDim.x) {
-    const int j = A.perm[k];
+    const int j = perm[k];
     bad |= (j < 0 || j >= K);
   }
   if (__syncthreads_or(bad)) {
@@ -684,7 +686,7 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
   }
   // prologue: a(perm[0]) and a(perm[0])'D in full
   {
-    const int j0 = A.perm[0];
+    const int j0 = perm[0];
     for (int k = tid; k < A.Kp; k += blockDim.x) S.v_s[k] = S.v_entry(k, j0, -1);
     __syncthreads();
     S.next_partials(j0, -1, A.avec, A.aDbuf, tid, blockDim.x);
@@ -693,9 +695,9 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
     if (!S.barrier()) return;
   }
   for (int jj = 0; jj < K; ++jj) {
-    const int j = A.perm[jj];
-    const int prev = jj > 0 ? A.perm[jj - 1] : -1;
-    const int jn = jj + 1 < K ? A.perm[jj + 1] : -1;
+    const int j = perm[jj];
+    const int prev = jj > 0 ? perm[jj - 1] : -1;
+    const int jn = jj + 1 < K ? perm[jj + 1] : -1;
     float* av_next = A.avec + ((jj + 1) % 3) * n;
     float* av_clear = A.avec + ((jj + 2) % 3) * n;
     float* ad_next = A.aDbuf + ((jj + 1) & 1) * A.Kp;
@@ -787,7 +789,7 @@ cudaError_t launch_update_sweep(const UpdateArgs& a, cudaStream_t st) {
   if (a.N <= 0) return cudaSuccess;
   SweepArgs s;
   s.n = a.n; s.K = a.K; s.Kp = a.Kp; s.T = a.T; s.N = a.N; s.X = a.X; s.D = a.D; s.idx = a.idx;
-  s.coef = a.coef; s.nnz = a.nnz; s.perm = a.perm; s.max_signals = a.max_signals;
+  s.coef = a.coef; s.nnz = a.nnz; s.perm = a.perm; s.iter_ctr = a.iter_ctr; s.max_signals = a.max_signals;
   s.list = a.list; s.start = a.start; s.Y = a.Y; s.gn2 = a.gn2; s.C = a.C; s.G = a.G; s.P = a.P;
   s.avec = a.avec; s.aDbuf = a.aD; s.part = a.part; s.unused = a.unused; s.bitmap = a.bitmap;
   s.replaced = a.replaced; s.counter = a.counter; s.usecount = a.usecount; s.barrier = a.barrier;

@@ -4,3 +4,4 @@ Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU legs may imp
 package, as the checker.  The product library (``ksvd_gb300``) never imports it.
 """
 from .oracle import *  # noqa: F401,F403
+from . import adjoint  # noqa: F401

@@ -1,0 +1,98 @@
+"""Batched Batch-OMP (ksvd_batched_omp through the C ABI): many independent dictionaries of
+different n and K = 4n, uneven signal counts, error-constrained supports of 1..64 atoms, in one
+persistent launch with a device work queue.  Every problem must give exactly what the
+single-problem call gives on the same inputs (same kernels, same arithmetic), and agree with the
+FP64 oracle's error-constrained OMP on >= 99.9% of supports."""
+import numpy as np
+import pytest
+
+from conftest import rel_rmse, support_match_vec
+
+pytestmark = pytest.mark.gpu
+
+
+def make_problems(seed, sizes):
+    rng = np.random.default_rng(seed)
+    out = []
+    for n, N in sizes:
+        K = 4 * n
+        D0 = rng.standard_normal((n, K))
+        D0 /= np.linalg.norm(D0, axis=0)
+        X = np.zeros((n, N))
+        ts = rng.integers(1, min(48, n // 2) + 1, N)
+        snr = rng.uniform(15, 30, N)
+        for s in range(N):
+            S = rng.choice(K, ts[s], replace=False)
+            X[:, s] = D0[:, S] @ rng.standard_normal(ts[s])
+        sig = np.linalg.norm(X, axis=0) / np.sqrt(n) * 10 ** (-snr / 20)
+        X += rng.standard_normal((n, N)) * sig
+        D = rng.standard_normal((n, K))                      # a perturbed dictionary to code with
+        D = D0 + 0.3 * D / np.sqrt(n)
+        D /= np.linalg.norm(D, axis=0)
+        eps2 = (n * sig ** 2 * 1.1).astype(np.float32)       # stop near the noise floor
+        out.append(dict(n=n, K=K, N=N, T=min(64, n), X=X.astype(np.float32),
+                        D=D.astype(np.float32), eps2=eps2))
+    return out
+
+
+def test_batched_omp_matches_single_and_oracle(oracle_mod, cuda):
+    import torch
+
+    from ksvd_gb300 import Handle
+
+    probs = make_problems(21, [(32, 900), (64, 2500), (128, 400), (256, 1500), (64, 1),
+                               (128, 3000), (32, 5000)])
+    dev = []
+    for q in probs:
+        dev.append(dict(D=torch.from_numpy(np.ascontiguousarray(q["D"].T)).to(cuda),
+                        X=torch.from_numpy(np.ascontiguousarray(q["X"].T)).to(cuda),
+                        eps2=torch.from_numpy(q["eps2"]).to(cuda), T=q["T"]))
+    hb = Handle(1, 1, 1)
+    outs = hb.batched_omp(dev)
+    hb.synchronize()
+    sizes = []
+    for q, d, (idx, coef, nnz) in zip(probs, dev, outs):
+        h = Handle(q["n"], q["K"], q["T"])
+        i1, c1, n1 = h.omp(d["D"], d["X"], eps2=d["eps2"])
+        h.synchronize()
+        assert torch.equal(nnz, n1) and torch.equal(idx, i1) and torch.equal(coef, c1)
+        D64, X64 = q["D"].astype(np.float64), q["X"].astype(np.float64)
+        G, A0 = oracle_mod.gram(D64), oracle_mod.dtx(D64, X64)
+        xn2 = np.sum(X64 * X64, 0)
+        ri, rc, rn = oracle_mod.omp(G, A0, q["T"], xnorm2=xn2, eps2=q["eps2"].astype(np.float64))
+        gi, gn = idx.cpu().numpy(), nnz.cpu().numpy()
+        if q["N"] >= 100:
+            assert support_match_vec(gi, gn, ri, rn) >= 0.999
+            ok = (gn == rn)
+            assert rel_rmse(coef.cpu().numpy()[ok], rc[ok]) <= 1e-4
+        sizes.append(gn)
+        h.close()
+    allsz = np.concatenate(sizes)
+    assert allsz.min() >= 1 and allsz.max() > 30          # uneven supports really were exercised
+    hb.close()
+
+
+def test_batched_omp_t_sparse_and_empty(cuda):
+    """T-sparse jobs (no error targets) next to an empty problem; invalid sizes are refused."""
+    import torch
+
+    from ksvd_gb300 import Handle, KsvdError
+
+    probs = make_problems(5, [(64, 700), (32, 300)])
+    dev = [dict(D=torch.from_numpy(np.ascontiguousarray(q["D"].T)).to(cuda),
+                X=torch.from_numpy(np.ascontiguousarray(q["X"].T)).to(cuda), T=5) for q in probs]
+    dev.insert(1, dict(D=dev[0]["D"], X=dev[0]["X"][:0], T=5))
+    hb = Handle(1, 1, 1)
+    outs = hb.batched_omp(dev)
+    for d, (idx, coef, nnz) in zip(dev, outs):
+        if d["X"].shape[0] == 0:
+            continue
+        h = Handle(d["D"].shape[1], d["D"].shape[0], 5)
+        i1, c1, n1 = h.omp(d["D"], d["X"])
+        assert torch.equal(idx, i1) and torch.equal(coef, c1) and torch.equal(nnz, n1)
+        assert int(nnz.min()) == 5
+        h.close()
+    bad = [dict(D=dev[0]["D"], X=dev[0]["X"], T=65)]
+    with pytest.raises(KsvdError):
+        hb.batched_omp(bad)
+    hb.close()

@@ -313,3 +313,38 @@ def test_full_size_properties(oracle_mod, cuda):
     ri, rc, rn = oracle_mod.omp(oracle_mod.gram(Dn64), oracle_mod.dtx(Dn64, Xs64), 16)
     assert support_match_vec(i2.cpu().numpy(), n2.cpu().numpy(), ri, rn) >= SUPPORT_MIN
     h.close()
+
+
+@pytest.mark.parametrize("precision", ["fp32", "mixed"])
+def test_iterate_graph_replay_matches_plain_launches(cuda, precision):
+    """KSVD_FLAG_GRAPH: iterations 2..iters replay a captured CUDA graph of one iteration; the
+    results equal the plain-launch run's, and a second call on the same buffers reuses the graph."""
+    import torch
+
+    from ksvd_gb300 import Handle, datagen, random_permutation
+
+    p = datagen.make_problem("cfg0", N=4000, dict_from="extra")
+    c = p["cfg"]
+    X = torch.from_numpy(np.ascontiguousarray(np.asarray(p["X"], np.float32).T)).to(cuda)
+    D0 = torch.from_numpy(np.ascontiguousarray(np.asarray(p["D"], np.float32).T)).to(cuda)
+    perms = np.stack([random_permutation(3, it, c.K) for it in range(4)])
+    res = []
+    for graph in (False, True):
+        h = Handle(c.n, c.K, c.T, precision=precision, graph=graph)
+        D = D0.clone()
+        idx, coef, nnz, rmse = h.iterate(D, X, 4, perms=perms)
+        h.synchronize()
+        res.append((D.clone(), idx.clone(), coef.clone(), rmse, h.graph_replays()))
+        if graph:
+            D2 = D0.clone()
+            out = (idx, coef, nnz)
+            _, _, _, rmse2 = h.iterate(D2, X, 4, perms=perms, out=out)
+            h.synchronize()
+            assert h.graph_replays() == 6                 # the cached graph was replayed again
+            np.testing.assert_allclose(rmse2, rmse, rtol=1e-6)
+        h.close()
+    (Da, ia, ca, ra, ga), (Db, ib, cb, rb, gb) = res
+    assert ga == 0 and gb == 3
+    np.testing.assert_allclose(rb, ra, rtol=1e-6)
+    assert rel_rmse(Db.cpu().numpy(), Da.cpu().numpy()) <= 1e-5
+    assert (ia == ib).float().mean().item() >= 0.999

@@ -340,3 +340,33 @@ def test_ksvd_reduces_error(oracle_mod):
     Dn, idx, coef, nnz, rmse = oracle_mod.ksvd(p["X"], p["D"], 8, 4, perms)
     assert np.all(np.diff(rmse) < 0)
     np.testing.assert_allclose(np.linalg.norm(Dn, axis=0), 1.0, atol=1e-12)
+
+
+def test_adjoint_formula_matches_finite_differences():
+    """The FP64 adjoint of fixed-support coding (oracle/adjoint.py) against central differences
+    (h=1e-3) of L = ||X - D Gamma||^2 + 1/2 ||W Gamma||^2, with ragged supports (0..T atoms)."""
+    from oracle import adjoint as A
+
+    rng = np.random.default_rng(11)
+    n, K, N, T = 16, 40, 200, 5
+    D = rng.standard_normal((n, K))
+    D /= np.linalg.norm(D, axis=0)
+    X = rng.standard_normal((n, N))
+    nnz = rng.integers(0, T + 1, N).astype(np.int32)
+    idx = np.full((N, T), -1, np.int32)
+    for s in range(N):
+        idx[s, : nnz[s]] = rng.choice(K, nnz[s], replace=False)
+    W = rng.standard_normal((10, K))
+    dD, dX, coef, _ = A.grad_w(D, X, idx, nnz, W)
+    # coefficients: least squares on the support
+    s = int(np.argmax(nnz))
+    want = np.linalg.lstsq(D[:, idx[s, : nnz[s]]], X[:, s], rcond=None)[0]
+    np.testing.assert_allclose(coef[s, : nnz[s]], want, rtol=1e-10, atol=1e-12)
+    ent = [(int(rng.integers(n)), int(rng.integers(K))) for _ in range(60)]
+    fd = A.fd_grad_D(D, X, idx, nnz, W, ent)
+    an = np.array([dD[i, j] for i, j in ent])
+    assert np.abs(fd - an).max() <= 1e-5 * np.abs(an).max()
+    ent = [(int(rng.integers(n)), int(rng.integers(N))) for _ in range(60)]
+    fd = A.fd_grad_X(D, X, idx, nnz, W, ent)
+    an = np.array([dX[i, s] for i, s in ent])
+    assert np.abs(fd - an).max() <= 1e-8 * np.abs(an).max()
