@@ -231,6 +231,16 @@ typedef struct ksvd_problem {
 KSVD_API ksvd_status ksvd_batched_omp(ksvd_handle* handle, const ksvd_problem* probs,
                                       int32_t nprob);
 
+/* iters K-SVD iterations of every problem (each N >= 1): per iteration ONE persistent Batch-OMP
+ * launch over all problems (as ksvd_batched_omp), then every problem's dictionary update, error
+ * and clearDict concurrently on its own stream (the cooperative sweeps share the SMs in
+ * proportion to N*T).  D is normalised first and updated in place; idx/coef/nnz hold the last
+ * iteration's code; rmse (host, nullable) gets nprob x iters values, problem-major.  The
+ * handle's mu_thresh, use_thresh, max_replace_signals and seed apply to every problem (FP32).
+ * Replaces a host loop of KSVD::ExecuteIterations calls (S/KSVD.cu:55-131), one per dictionary. */
+KSVD_API ksvd_status ksvd_batched_iterate(ksvd_handle* handle, ksvd_problem* probs,
+                                          int32_t nprob, int32_t iters, double* rmse);
+
 /* ---- whole algorithm ----------------------------------------------------------------------- */
 
 /* iters K-SVD iterations: normcols(D) once, then per iteration Gram, D'X, Batch-OMP, dictionary

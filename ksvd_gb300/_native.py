@@ -32,6 +32,7 @@ EXPORTS = (
     "ksvd_iterate_host", "ksvd_dense_gamma", "ksvd_synchronize", "ksvd_read_stage_times",
     "ksvd_rmse_noalloc", "ksvd_code_fixed", "ksvd_code_backward",
     "ksvd_refine_coefs", "ksvd_batched_omp", "ksvd_graph_replays",
+    "ksvd_batched_iterate",
 )
 
 FLAG_PROFILE = 1
@@ -104,6 +105,7 @@ def _declare(lib):
         "ksvd_refine_coefs": (st, [vp, vp, vp, i64, vp, vp, vp, vp]),
         "ksvd_batched_omp": (st, [vp, vp, i32]),
         "ksvd_graph_replays": (i64, [vp]),
+        "ksvd_batched_iterate": (st, [vp, vp, i32, i32, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -288,11 +288,7 @@ class Handle:
                                                  _ptr(dD), _ptr(dX)))
         return dD, dX
 
-    def batched_omp(self, problems):
-        """Batch-OMP of many independent problems in one persistent launch.
-
-        ``problems``: sequence of dicts with D (K, n) and X (N, n) float32 device tensors, T, and
-        optional eps2 (N,) float32 (error targets).  Returns [(idx, coef, nnz), ...]."""
+    def _problems(self, problems, out=None):
         import torch
 
         arr = (_native.Problem * max(len(problems), 1))()
@@ -303,9 +299,12 @@ class Handle:
             N = X.shape[0]
             _need(D, "D", torch.float32, (K, n))
             _need(X, "X", torch.float32, (N, n))
-            idx = torch.empty((N, T), dtype=torch.int32, device=X.device)
-            coef = torch.empty((N, T), dtype=torch.float32, device=X.device)
-            nnz = torch.empty((N,), dtype=torch.int32, device=X.device)
+            if out is not None:
+                idx, coef, nnz = out[i]
+            else:
+                idx = torch.empty((N, T), dtype=torch.int32, device=X.device)
+                coef = torch.empty((N, T), dtype=torch.float32, device=X.device)
+                nnz = torch.empty((N,), dtype=torch.int32, device=X.device)
             e = q.get("eps2")
             if e is not None:
                 _need(e, "eps2", torch.float32, (N,))
@@ -313,8 +312,25 @@ class Handle:
                                      e.data_ptr() if e is not None else None, idx.data_ptr(),
                                      coef.data_ptr(), nnz.data_ptr())
             outs.append((idx, coef, nnz))
+        return arr, outs
+
+    def batched_omp(self, problems, out=None):
+        """Batch-OMP of many independent problems in one persistent launch.
+
+        ``problems``: sequence of dicts with D (K, n) and X (N, n) float32 device tensors, T, and
+        optional eps2 (N,) float32 (error targets).  Returns [(idx, coef, nnz), ...]."""
+        arr, outs = self._problems(problems, out)
         self._check(self._lib.ksvd_batched_omp(self._h, arr, len(problems)))
         return outs
+
+    def batched_iterate(self, problems, iters, out=None):
+        """K-SVD on many independent problems (dicts as for batched_omp; each D is normalised
+        and updated in place).  Returns ([(idx, coef, nnz), ...], rmse (nprob, iters))."""
+        arr, outs = self._problems(problems, out)
+        rmse = np.zeros((max(len(problems), 1), max(iters, 1)), np.float64)
+        self._check(self._lib.ksvd_batched_iterate(self._h, arr, len(problems), int(iters),
+                                                   rmse.ctypes.data_as(C.c_void_p)))
+        return outs, rmse[:len(problems), :iters]
 
     def dense_gamma(self, idx, coef, nnz):
         import torch

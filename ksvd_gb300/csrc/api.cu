@@ -60,6 +60,12 @@ struct ksvd_handle {
   GraphKey gkey{};
   bool graph_broken = false;
   int64_t graph_replays = 0;
+  // batched K-SVD: one child handle (own stream and workspace) per problem
+  std::vector<ksvd_handle*> kids;
+  std::vector<cudaStream_t> kid_streams;
+  std::vector<cudaEvent_t> kid_events;
+  cudaEvent_t fork_ev = nullptr;
+  int sweep_ctas = 0;   // CTAs of this handle's cooperative sweep (0: one per SM)
   // host copies of the batched call's tables (kept alive for the asynchronous uploads)
   std::vector<ksvd::GemmDesc> batch_descs;
   std::vector<ksvd::OmpJob> batch_jobs;
@@ -317,6 +323,7 @@ ksvd_status update_ws(ksvd_handle* h, int64_t N, UpdateArgs& u) {
   KSVD_TRY(ensure(h, B_DEVERR, 1, &u.dev_err));
   u.n = n; u.K = h->p.K; u.Kp = Kp; u.T = h->p.T; u.N = N;
   u.max_signals = h->p.max_replace_signals;
+  u.sweep_ctas = h->sweep_ctas;
   return KSVD_OK;
 }
 
@@ -515,6 +522,13 @@ void ksvd_destroy(ksvd_handle* h) {
   for (auto& b : h->bufs)
     if (b.p) cudaFree(b.p);
   for (auto e : h->ev_pool) cudaEventDestroy(e);
+  for (auto k : h->kids) ksvd_destroy(k);
+  for (auto st : h->kid_streams) {
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+  }
+  for (auto e : h->kid_events) cudaEventDestroy(e);
+  if (h->fork_ev) cudaEventDestroy(h->fork_ev);
   if (h->gexec) cudaGraphExecDestroy(h->gexec);
   if (h->gstream) {
     cudaStreamSynchronize(h->gstream);
@@ -699,6 +713,132 @@ ksvd_status ksvd_batched_omp(ksvd_handle* h, const ksvd_problem* probs, int32_t 
   StageScope sc(h, KSVD_STAGE_OMP);
   KSVD_CK(h, launch_omp_batched(jdev, nj, chunks, tmax, queue, de, h->stream));
   return KSVD_OK;
+}
+
+namespace {
+
+// Child handle i of a batched call: sizes (n, K, T) of problem i, the parent's other parameters,
+// its own non-blocking stream and completion event.  Reused while the sizes stay the same.
+ksvd_status batch_child(ksvd_handle* h, int i, const ksvd_problem& q, ksvd_handle** out) {
+  while ((int)h->kids.size() <= i) {
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    KSVD_CK(h, cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    h->kid_streams.push_back(st);
+    KSVD_CK(h, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    h->kid_events.push_back(ev);
+    h->kids.push_back(nullptr);
+  }
+  ksvd_handle*& k = h->kids[i];
+  if (k && (k->p.n != q.n || k->p.K != q.K || k->p.T != q.T)) {
+    ksvd_destroy(k);
+    k = nullptr;
+  }
+  if (!k) {
+    ksvd_params p = h->p;
+    p.n = q.n; p.K = q.K; p.T = q.T;
+    p.precision = KSVD_PREC_FP32;
+    p.flags = 0;
+    p.seed = h->p.seed + 0x9E3779B97F4A7C15ULL * (uint64_t)(i + 1);
+    const ksvd_status st = ksvd_create(&k, &p, h->kid_streams[i]);
+    if (st != KSVD_OK) return fail(h, st, "creating a batched problem's handle failed%s");
+  }
+  *out = k;
+  return KSVD_OK;
+}
+
+// Parent stream -> every child stream (fork) and back (join).
+ksvd_status batch_fork(ksvd_handle* h, int n) {
+  if (!h->fork_ev) KSVD_CK(h, cudaEventCreateWithFlags(&h->fork_ev, cudaEventDisableTiming));
+  KSVD_CK(h, cudaEventRecord(h->fork_ev, h->stream));
+  for (int i = 0; i < n; ++i) KSVD_CK(h, cudaStreamWaitEvent(h->kid_streams[i], h->fork_ev, 0));
+  return KSVD_OK;
+}
+ksvd_status batch_join(ksvd_handle* h, int n) {
+  for (int i = 0; i < n; ++i) {
+    KSVD_CK(h, cudaEventRecord(h->kid_events[i], h->kid_streams[i]));
+    KSVD_CK(h, cudaStreamWaitEvent(h->stream, h->kid_events[i], 0));
+  }
+  return KSVD_OK;
+}
+
+ksvd_status kid_error(ksvd_handle* h, ksvd_handle* k, ksvd_status s) {
+  if (s != KSVD_OK && h != k) h->err = "batched problem: " + k->err;
+  return s;
+}
+
+}  // namespace
+
+// K-SVD on many independent problems.  Per iteration: ONE persistent Batch-OMP launch over all
+// problems (ksvd_batched_omp), then every problem's dictionary update, error and clearDict on
+// its own stream, concurrently; the cooperative sweeps share the SMs in proportion to each
+// problem's work (N*T), one CTA per SM in total, so they all fit on the GPU at once.
+ksvd_status ksvd_batched_iterate(ksvd_handle* h, ksvd_problem* probs, int32_t nprob,
+                                 int32_t iters, double* rmse) {
+  if (!h || nprob < 0 || (nprob > 0 && !probs) || iters < 0) return KSVD_ERR_INVALID_ARGUMENT;
+  if (nprob == 0 || iters == 0) return KSVD_OK;
+  if (iters > 1024) return fail(h, KSVD_ERR_UNSUPPORTED, "at most 1024 iterations per call%s");
+  for (int32_t i = 0; i < nprob; ++i)
+    if (probs[i].N < 1)
+      return fail(h, KSVD_ERR_INVALID_ARGUMENT, "every batched K-SVD problem needs N >= 1%s");
+  // workspace of the children first: the sweep CTA shares, dictionaries, permutations
+  int sms = 0;
+  KSVD_CK(h, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
+  double work = 0;
+  for (int32_t i = 0; i < nprob; ++i) work += (double)probs[i].N * probs[i].T;
+  std::vector<ksvd_handle*> ks(nprob);
+  std::vector<float*> Dp(nprob);
+  std::vector<int32_t*> pd(nprob);
+  std::vector<double*> rd(nprob);
+  std::vector<int32_t*> cd(nprob);
+  std::vector<ksvd_problem> inner(probs, probs + nprob);
+  int budget = sms - nprob;   // every problem has one CTA; the rest go by work
+  for (int32_t i = 0; i < nprob; ++i) {
+    KSVD_TRY(batch_child(h, i, probs[i], &ks[i]));
+    ksvd_handle* k = ks[i];
+    const int extra = budget > 0 ? (int)((double)budget * probs[i].N * probs[i].T / work) : 0;
+    k->sweep_ctas = std::max(1, 1 + extra);
+  }
+  KSVD_TRY(batch_fork(h, nprob));
+  for (int32_t i = 0; i < nprob; ++i) {
+    ksvd_handle* k = ks[i];
+    if (bad_ptr(probs[i].D) || bad_ptr(probs[i].X))
+      return fail(h, KSVD_ERR_INVALID_ARGUMENT, "batched problem with a null pointer%s");
+    KSVD_TRY(kid_error(h, k, load_dict(k, probs[i].D, &Dp[i])));
+    KSVD_TRY(kid_error(h, k, ensure(k, B_RMSE, 1024, &rd[i])));
+    KSVD_TRY(kid_error(h, k, ensure(k, B_CLEARED, 1, &cd[i])));
+    KSVD_TRY(kid_error(h, k, upload_perm(k, nullptr, iters, &pd[i])));
+    KSVD_CK(h, launch_normcols(Dp[i], k->p.n, k->p.K, k->stream));   // KSVD.cu:57
+    inner[i].D = Dp[i];             // OMP codes with the children's working dictionaries
+  }
+  KSVD_TRY(batch_join(h, nprob));
+  for (int32_t it = 0; it < iters; ++it) {
+    KSVD_TRY(ksvd_batched_omp(h, inner.data(), nprob));
+    KSVD_TRY(batch_fork(h, nprob));
+    for (int32_t i = 0; i < nprob; ++i) {
+      ksvd_handle* k = ks[i];
+      const ksvd_problem& q = probs[i];
+      float* G = nullptr;
+      KSVD_TRY(kid_error(h, k, ensure(k, B_G, (size_t)k->Kp * k->Kp, &G)));
+      KSVD_TRY(kid_error(h, k, run_update(k, Dp[i], q.X, q.N, q.idx, q.coef, q.nnz,
+                                          pd[i] + (size_t)it * q.K)));
+      KSVD_TRY(kid_error(h, k, run_error(k, Dp[i], q.X, q.N, q.idx, q.coef, q.nnz, rd[i] + it)));
+      KSVD_TRY(kid_error(h, k, gram_padded(k, Dp[i], G)));
+      KSVD_TRY(kid_error(h, k, run_clear(k, Dp[i], G, q.X, q.N, cd[i])));
+    }
+    KSVD_TRY(batch_join(h, nprob));
+  }
+  KSVD_TRY(batch_fork(h, nprob));
+  for (int32_t i = 0; i < nprob; ++i) {
+    KSVD_TRY(kid_error(h, ks[i], store_dict(ks[i], Dp[i], probs[i].D)));
+    if (rmse)
+      KSVD_CK(h, cudaMemcpyAsync(rmse + (size_t)i * iters, rd[i], sizeof(double) * iters,
+                                 cudaMemcpyDeviceToHost, ks[i]->stream));
+  }
+  KSVD_TRY(batch_join(h, nprob));
+  KSVD_CK(h, cudaStreamSynchronize(h->stream));
+  for (int32_t i = 0; i < nprob; ++i) KSVD_TRY(kid_error(h, ks[i], check_dev_err(ks[i])));
+  return check_dev_err(h);
 }
 
 ksvd_status ksvd_update_dictionary(ksvd_handle* h, float* D, const float* X, int64_t N,

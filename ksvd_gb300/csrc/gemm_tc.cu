@@ -106,6 +106,7 @@ struct TcParams {
   int64_t Ncols;  // columns of C written (signals)
   int nk;         // inner chunks of 64
   int passes;     // 1 or 3
+  int mtiles;     // atom tiles (grid = mtiles x signal tiles, atom tile fastest)
   int* dev_err;
 };
 
@@ -123,8 +124,10 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_constant
   int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * TM;
-  const int64_t n0 = (int64_t)blockIdx.x * TN;
+  // atom tiles vary fastest, so the CTAs sharing a signal tile run together and the tile is read
+  // from HBM once (the others hit L2)
+  const int m0 = (int)(blockIdx.x % P.mtiles) * TM;
+  const int64_t n0 = (int64_t)(blockIdx.x / P.mtiles) * TN;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -341,9 +344,9 @@ cudaError_t launch_gemm_tn_bf16(const TcOperand& A, const TcOperand& B, float* C
   P.dev_err = dev_err;
   const int64_t gx = (Ncols + TN - 1) / TN;
   const int gy = (M + TM - 1) / TM;
-  if (gx > 0x7fffffffLL || gy > 65535) return cudaErrorInvalidValue;
-  gemm_tc_kernel<<<dim3((unsigned)gx, (unsigned)gy), 128, SMEM_BYTES, st>>>(ma_hi, ma_lo, mb_hi,
-                                                                             mb_lo, P);
+  if (gx * gy > 0x7fffffffLL) return cudaErrorInvalidValue;
+  P.mtiles = gy;
+  gemm_tc_kernel<<<(unsigned)(gx * gy), 128, SMEM_BYTES, st>>>(ma_hi, ma_lo, mb_hi, mb_lo, P);
   return cudaGetLastError();
 }
 

@@ -65,6 +65,7 @@ struct UpdateArgs {
   const int32_t* perm;   // K (or iters x K with iter_ctr)
   const int* iter_ctr;   // nullable: use perm + (*iter_ctr) * K (graph replays)
   int max_signals;
+  int sweep_ctas;        // CTAs of the cooperative sweep (0: one per SM)
   // workspace
   int32_t* list;         // total entries (signal*T + slot), per-atom ascending signal order
   int64_t* start;        // Kp + 1

@@ -804,7 +804,8 @@ cudaError_t launch_update_sweep(const UpdateArgs& a, cudaStream_t st) {
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSweepThreads, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorCooperativeLaunchTooLarge;
-    const int grid = sweep_grid_size();
+    const int full = sweep_grid_size();
+    const int grid = a.sweep_ctas > 0 && a.sweep_ctas < full ? a.sweep_ctas : full;
     void* args[] = {&s};
     return cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(kSweepThreads), args,
                                        smem, st);

@@ -8,6 +8,8 @@ named configurations:
 * ``cfg1``  n=200, K=512,  N=200,000,   T=10, 20 iterations, 10 dB, AR(1) rho=0.9 atoms,
   row means removed (Matlab/remmean.m:13-15)
 * ``cfg2``  n=256, K=1024, N=1,000,000, T=16, 10 iterations, 25 dB (the headline workload)
+* ``cfg3``  64 independent problems, n uniform in {32, 64, 128, 256}, K = 4n, N uniform in
+  10k..200k each, error-constrained coding (``make_batched``)
 * ``cfg4``  n=128, K=512,  N=100,000,   T=12 (fixed-support coding adjoint)
 * ``ref``   n=300, K=9,    N=3,600,     T=6,  30 iterations (the reference's own shape)
 
@@ -147,3 +149,48 @@ def _make_problem_torch(cfg, N, seed, device):
     D = X[pick].clone()
     D /= D.norm(dim=1, keepdim=True)
     return dict(X=X, D=D, cfg=cfg)
+
+
+def make_batched(nprob=64, seed=SEED_BASE + 3, device="cuda", n_choices=(32, 64, 128, 256),
+                 n_range=(10_000, 200_000), scale=1.0):
+    """The batched workload: ``nprob`` independent problems with n uniform in ``n_choices``,
+    K = 4n, N uniform in ``n_range`` (times ``scale``).  Each signal is a sparse combination of
+    T_s ~ U[1, min(48, n/2)] unit-norm N(0,1) atoms with N(0,1) coefficients plus white noise at
+    an SNR uniform in [15, 30] dB; its error target is eps^2 = 1.05 * n * sigma_s^2 (the
+    expected noise energy), so the coded supports spread over 1..64 atoms.  The coefficient
+    slots per signal are T = min(64, n).  The initial dictionary is K distinct signals,
+    normalised.  Returns a list of dicts (D (K, n), X (N, n), eps2 (N,), T) of device tensors."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    out = []
+    for _ in range(nprob):
+        n = int(rng.choice(n_choices))
+        K = 4 * n
+        N_full = int(rng.integers(n_range[0], n_range[1] + 1))
+        N = max(K, int(N_full * scale))
+        tmax = min(48, n // 2)
+        D0 = torch.from_numpy(_unit_columns(rng.standard_normal((n, K))).T.astype(np.float32))
+        D0 = D0.to(device)
+        X = torch.empty((N, n), dtype=torch.float32, device=device)
+        eps2 = torch.empty((N,), dtype=torch.float32, device=device)
+        chunk = 1 << 14
+        for s0 in range(0, N, chunk):
+            m = min(N, s0 + chunk) - s0
+            t = torch.randint(1, tmax + 1, (m, 1), generator=g, device=device)
+            keys = torch.rand((m, K), generator=g, device=device)
+            top = keys.topk(tmax, dim=1).indices                      # (m, tmax) distinct
+            live = torch.arange(tmax, device=device)[None, :] < t
+            gam = torch.randn((m, tmax), generator=g, device=device) * live
+            clean = torch.einsum("mtr,mt->mr", D0[top], gam)
+            snr = 15 + 15 * torch.rand((m, 1), generator=g, device=device)
+            sig = clean.norm(dim=1, keepdim=True) / math.sqrt(n) * 10 ** (-snr / 20)
+            X[s0:s0 + m] = clean + torch.randn((m, n), generator=g, device=device) * sig
+            eps2[s0:s0 + m] = (1.05 * n * sig * sig)[:, 0]
+        pick = torch.randperm(N, generator=g, device=device)[:K]
+        D = X[pick].clone()
+        D /= D.norm(dim=1, keepdim=True)
+        out.append(dict(D=D, X=X, eps2=eps2, T=min(64, n), n=n, K=K, N=N, N_full=N_full))
+    return out

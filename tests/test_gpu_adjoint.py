@@ -164,7 +164,7 @@ def test_iterate_refine_final(cuda):
                      nnz.cpu().numpy(), rmse))
         h.close()
     (Da, ia, ca, na, ra), (Db, ib, cb, nb, rb) = outs
-    np.testing.assert_allclose(ra, rb, rtol=1e-6)
+    np.testing.assert_allclose(ra, rb, rtol=1e-4)      # two runs: float atomics reorder sums
     X64 = X.double().cpu().numpy().T
     want = A.code_fixed(Db, X64, ib, nb)
     assert rel_rmse(cb, want) <= 1e-6

@@ -27,7 +27,7 @@ def make_problems(seed, sizes):
         sig = np.linalg.norm(X, axis=0) / np.sqrt(n) * 10 ** (-snr / 20)
         X += rng.standard_normal((n, N)) * sig
         D = rng.standard_normal((n, K))                      # a perturbed dictionary to code with
-        D = D0 + 0.3 * D / np.sqrt(n)
+        D = D0 + 0.05 * D / np.sqrt(n)
         D /= np.linalg.norm(D, axis=0)
         eps2 = (n * sig ** 2 * 1.1).astype(np.float32)       # stop near the noise floor
         out.append(dict(n=n, K=K, N=N, T=min(64, n), X=X.astype(np.float32),
@@ -95,4 +95,40 @@ def test_batched_omp_t_sparse_and_empty(cuda):
     bad = [dict(D=dev[0]["D"], X=dev[0]["X"], T=65)]
     with pytest.raises(KsvdError):
         hb.batched_omp(bad)
+    hb.close()
+
+
+def test_batched_iterate_matches_single_problem_runs(cuda):
+    """ksvd_batched_iterate (one persistent OMP launch per iteration, every problem's update on its
+    own stream with a share of the SMs) against ksvd_iterate run on each problem alone with the
+    same permutations: per-iteration RMSE within 1e-4 relative, dictionaries within 1e-3."""
+    import torch
+
+    from ksvd_gb300 import Handle, random_permutation
+
+    probs = make_problems(8, [(32, 3000), (64, 2000), (128, 1500), (256, 1200), (64, 5000)])
+    iters = 2
+    seed = 0x4B535644
+    dev = []
+    for q in probs:
+        dev.append(dict(D=torch.from_numpy(np.ascontiguousarray(q["D"].T)).to(cuda),
+                        X=torch.from_numpy(np.ascontiguousarray(q["X"].T)).to(cuda), T=6))
+    D0 = [d["D"].clone() for d in dev]
+    hb = Handle(1, 1, 1, seed=seed)
+    outs, rmse = hb.batched_iterate(dev, iters)
+    hb.synchronize()
+    assert rmse.shape == (len(probs), iters) and np.all(rmse[:, 1] <= rmse[:, 0] * 1.01)
+    for i, (q, d) in enumerate(zip(probs, dev)):
+        kseed = (seed + 0x9E3779B97F4A7C15 * (i + 1)) & 0xFFFFFFFFFFFFFFFF
+        perms = np.stack([random_permutation(kseed, it, q["K"]) for it in range(iters)])
+        h = Handle(q["n"], q["K"], 6)
+        D1 = D0[i].clone()
+        _, _, _, r1 = h.iterate(D1, d["X"], iters, perms=perms)
+        h.synchronize()
+        np.testing.assert_allclose(rmse[i], r1, rtol=1e-4)
+        assert rel_rmse(d["D"].cpu().numpy(), D1.cpu().numpy()) <= 1e-3
+        h.close()
+    # a second call reuses the children (same sizes) and goes on from the updated dictionaries
+    outs2, rmse2 = hb.batched_iterate(dev, 1, out=outs)
+    assert np.all(rmse2[:, 0] <= rmse[:, -1] * 1.01)
     hb.close()
