@@ -336,6 +336,8 @@ def run_batched(args):
                               "omp_ms": omp_ms, "gemm_ms": gemm_ms},
         "support_sizes": {"min": int(sizes.min()), "mean": float(sizes.mean()),
                           "max": int(sizes.max())},
+        "stage_ms_per_step_summed_over_problems": {
+            k: round(v[0] / args.steps, 3) for k, v in st.items() if v[1] > 0},
         "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
         "rmse_last_mean": float(np.mean(rmse[:, -1])),
     }

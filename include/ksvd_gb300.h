@@ -129,6 +129,19 @@ KSVD_API ksvd_status ksvd_random_permutation(uint64_t seed, int64_t iteration, i
 /* D <- D * diag(1/||d_k||), in place.  Replaces KSVD::normcols (KSVD.cu:267-286). */
 KSVD_API ksvd_status ksvd_normcols(ksvd_handle* handle, float* D);
 
+/* Preprocessing of the fMRI workflow: subtract from every row of X (n x N, device, in place) its
+ * mean over the N signals; mean (nullable, device, n floats) receives the means.  Sums are FP64
+ * in a fixed order (deterministic).  Replaces Matlab/remmean.m:13-15 run before the executable. */
+KSVD_API ksvd_status ksvd_remove_row_mean(ksvd_handle* handle, float* X, int64_t N, float* mean);
+
+/* Checkpoint/resume of the atom-order stream: ksvd_iterate without explicit permutations draws
+ * iteration i's order as ksvd_random_permutation(seed, draws + i, K) and then advances draws by
+ * the iteration count.  Saving draws with D and restoring it (with the same seed) continues a
+ * run with exactly the orders it would have used.  No reference counterpart (its orders come
+ * from unseeded std::random_shuffle, S/RandPermutation.cu:35-42). */
+KSVD_API int64_t ksvd_perm_draws(const ksvd_handle* handle);
+KSVD_API ksvd_status ksvd_set_perm_draws(ksvd_handle* handle, int64_t draws);
+
 /* G = D'D (K x K).  Replaces Multiplication::AT_times_B at KSVD.cu:64-73. */
 KSVD_API ksvd_status ksvd_gram(ksvd_handle* handle, const float* D, float* G);
 

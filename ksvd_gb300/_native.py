@@ -32,7 +32,7 @@ EXPORTS = (
     "ksvd_iterate_host", "ksvd_dense_gamma", "ksvd_synchronize", "ksvd_read_stage_times",
     "ksvd_rmse_noalloc", "ksvd_code_fixed", "ksvd_code_backward",
     "ksvd_refine_coefs", "ksvd_batched_omp", "ksvd_graph_replays",
-    "ksvd_batched_iterate",
+    "ksvd_batched_iterate", "ksvd_remove_row_mean", "ksvd_perm_draws", "ksvd_set_perm_draws",
 )
 
 FLAG_PROFILE = 1
@@ -106,6 +106,9 @@ def _declare(lib):
         "ksvd_batched_omp": (st, [vp, vp, i32]),
         "ksvd_graph_replays": (i64, [vp]),
         "ksvd_batched_iterate": (st, [vp, vp, i32, i32, vp]),
+        "ksvd_remove_row_mean": (st, [vp, vp, i64, vp]),
+        "ksvd_perm_draws": (i64, [vp]),
+        "ksvd_set_perm_draws": (st, [vp, i64]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -111,6 +111,25 @@ class Handle:
     def synchronize(self):
         self._check(self._lib.ksvd_synchronize(self._h))
 
+    def remove_row_mean(self, X):
+        """X (N, n) device tensor: subtract each of the n rows' mean over the signals, in place.
+        Returns the means (n,)."""
+        import torch
+
+        _need(X, "X", torch.float32, (X.shape[0], self.n))
+        mean = torch.empty((self.n,), dtype=torch.float32, device=X.device)
+        self._check(self._lib.ksvd_remove_row_mean(self._h, _ptr(X), X.shape[0], _ptr(mean)))
+        return mean
+
+    @property
+    def perm_draws(self) -> int:
+        """Atom orders drawn so far (saved with D for checkpoint/resume)."""
+        return int(self._lib.ksvd_perm_draws(self._h))
+
+    @perm_draws.setter
+    def perm_draws(self, v):
+        self._check(self._lib.ksvd_set_perm_draws(self._h, int(v)))
+
     def graph_replays(self) -> int:
         """Iterations ksvd_iterate ran as CUDA-graph replays on this handle."""
         return int(self._lib.ksvd_graph_replays(self._h))

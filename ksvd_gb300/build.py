@@ -19,6 +19,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB_NAME = "libksvd_gb300.so"
 LIB_PATH = os.path.join(OUT_DIR, LIB_NAME)
+CLI_SRC = os.path.join(HERE, "cli", "ksvd_cli.cpp")
+CLI_PATH = os.path.join(OUT_DIR, "ksvd")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -41,7 +43,7 @@ def _headers():
 
 def _fingerprint(flags):
     h = hashlib.sha256()
-    for p in _sources() + _headers():
+    for p in _sources() + _headers() + [CLI_SRC]:
         with open(p, "rb") as f:
             h.update(p.encode() + b"\0" + f.read())
     h.update(" ".join(flags).encode())
@@ -83,9 +85,24 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
     os.replace(tmp, LIB_PATH)
+    build_cli(nvcc)
     with open(stamp, "w") as f:
         f.write(fp)
     return LIB_PATH
+
+
+def build_cli(nvcc=None) -> str:
+    """The ``ksvd`` command-line program (host C++ over the library), next to the library."""
+    nvcc = nvcc or _nvcc()
+    tmp = CLI_PATH + ".tmp%d" % os.getpid()
+    cmd = [nvcc, "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), CLI_SRC, "-o", tmp,
+           "-L", OUT_DIR, "-lksvd_gb300", "-cudart", "shared",
+           "-Xlinker", "-rpath=$ORIGIN", "-Xlinker", "-rpath=/usr/local/cuda/lib64"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("CLI build failed:\n%s\n%s" % (r.stdout, r.stderr))
+    os.replace(tmp, CLI_PATH)
+    return CLI_PATH
 
 
 if __name__ == "__main__":

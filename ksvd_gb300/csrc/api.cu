@@ -77,7 +77,7 @@ enum BufId {
   B_DPAD, B_G, B_A0, B_XN2, B_LIST, B_START, B_BHIST, B_Y, B_GN2, B_C, B_AVEC, B_AD, B_PART,
   B_UNUSED, B_BITMAP, B_REPLACED, B_COUNTER, B_USE, B_BARRIER, B_ERR, B_PSUM, B_BVAL, B_BIDX,
   B_RMSE, B_M, B_MI, B_CLEARED, B_DEVERR, B_PERM, B_GPAD_IN, B_HX, B_HD, B_HIDX, B_HCOEF, B_HNNZ,
-  B_XHI, B_XLO, B_DHI, B_DLO, B_P, B_BG, B_BA0, B_BDESC, B_BJOB, B_BQUEUE, B_ITER, B_COUNT
+  B_XHI, B_XLO, B_DHI, B_DLO, B_P, B_BG, B_BA0, B_BDESC, B_BJOB, B_BQUEUE, B_ITER, B_RPART, B_RMEAN, B_COUNT
 };
 
 ksvd_status fail(ksvd_handle* h, ksvd_status s, const char* fmt, const char* detail = nullptr) {
@@ -550,6 +550,16 @@ ksvd_status ksvd_read_stage_times(ksvd_handle* h, ksvd_stage_times* out, int32_t
     out->calls[i] = h->stage_calls[i];
     if (reset) { h->stage_ms[i] = 0; h->stage_calls[i] = 0; }
   }
+  // a batched call's per-problem stages (their streams overlap: the sums exceed wall time)
+  for (auto k : h->kids) {
+    if (!k) continue;
+    ksvd_stage_times kt;
+    KSVD_TRY(ksvd_read_stage_times(k, &kt, reset));
+    for (int i = 0; i < 8; ++i) {
+      out->ms[i] += kt.ms[i];
+      out->calls[i] += kt.calls[i];
+    }
+  }
   return KSVD_OK;
 }
 
@@ -564,6 +574,27 @@ ksvd_status ksvd_synchronize(ksvd_handle* h) {
 ksvd_status ksvd_normcols(ksvd_handle* h, float* D) {
   if (!h || bad_ptr(D)) return KSVD_ERR_INVALID_ARGUMENT;
   KSVD_CK(h, launch_normcols(D, h->p.n, h->p.K, h->stream));
+  return KSVD_OK;
+}
+
+ksvd_status ksvd_remove_row_mean(ksvd_handle* h, float* X, int64_t N, float* mean) {
+  if (!h || bad_ptr(X) || N < 1) return KSVD_ERR_INVALID_ARGUMENT;
+  double* part = nullptr;
+  float* m = nullptr;
+  KSVD_TRY(ensure(h, B_RPART, (size_t)row_mean_blocks(N) * h->p.n, &part));
+  KSVD_TRY(ensure(h, B_RMEAN, (size_t)h->p.n, &m));
+  KSVD_CK(h, launch_remove_row_mean(X, h->p.n, N, part, m, h->stream));
+  if (mean)
+    KSVD_CK(h, cudaMemcpyAsync(mean, m, sizeof(float) * h->p.n, cudaMemcpyDeviceToDevice,
+                               h->stream));
+  return KSVD_OK;
+}
+
+int64_t ksvd_perm_draws(const ksvd_handle* h) { return h ? h->perm_draws : -1; }
+
+ksvd_status ksvd_set_perm_draws(ksvd_handle* h, int64_t draws) {
+  if (!h || draws < 0) return KSVD_ERR_INVALID_ARGUMENT;
+  h->perm_draws = draws;
   return KSVD_OK;
 }
 
@@ -738,7 +769,7 @@ ksvd_status batch_child(ksvd_handle* h, int i, const ksvd_problem& q, ksvd_handl
     ksvd_params p = h->p;
     p.n = q.n; p.K = q.K; p.T = q.T;
     p.precision = KSVD_PREC_FP32;
-    p.flags = 0;
+    p.flags = h->p.flags & KSVD_FLAG_PROFILE;
     p.seed = h->p.seed + 0x9E3779B97F4A7C15ULL * (uint64_t)(i + 1);
     const ksvd_status st = ksvd_create(&k, &p, h->kid_streams[i]);
     if (st != KSVD_OK) return fail(h, st, "creating a batched problem's handle failed%s");

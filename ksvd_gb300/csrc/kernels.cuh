@@ -130,6 +130,12 @@ struct ClearArgs {
 // m, mi: Kp scratch floats / ints (per-column largest off-diagonal G^2 and its row)
 cudaError_t launch_clear_dict(const ClearArgs& a, float* m, int* mi, cudaStream_t st);
 
+// X(r, :) -= mean of row r over the N signals (Matlab/remmean.m:13-15), FP64 sums in a fixed order.
+// part: row_mean_blocks(N) x n doubles of scratch; mean: n floats (out).
+int64_t row_mean_blocks(int64_t N);
+cudaError_t launch_remove_row_mean(float* X, int n, int64_t N, double* part, float* mean,
+                                   cudaStream_t st);
+
 // *ctr += 1 (one thread): the iteration counter that graph-replayed iterations index by.
 cudaError_t launch_advance_counter(int* ctr, cudaStream_t st);
 

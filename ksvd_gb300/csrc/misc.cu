@@ -89,8 +89,56 @@ cudaError_t launch_copy_pad_cols(const float* src, int n, int K, float* dst, int
 
 __global__ void advance_counter_kernel(int* c) { *c += 1; }
 
+// Row means of X (n x N column-major): block b sums rows over its chunk of kRowChunk signals in
+// FP64 (thread r owns rows r, r + blockDim, ...); partials land in part[b * n + r].
+constexpr int kRowChunk = 2048;
+__global__ void row_partial_kernel(const float* __restrict__ X, int n, int64_t N,
+                                   double* __restrict__ part) {
+  const int64_t s0 = (int64_t)blockIdx.x * kRowChunk;
+  const int64_t s1 = min(N, s0 + kRowChunk);
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    double acc = 0.0;
+    for (int64_t s = s0; s < s1; ++s) acc += (double)X[s * n + r];
+    part[(int64_t)blockIdx.x * n + r] = acc;
+  }
+}
+
+// mean[r] = (sum of the partials in block order) / N: deterministic, no atomics.
+__global__ void row_mean_kernel(const double* __restrict__ part, int64_t nblk, int n, int64_t N,
+                                float* __restrict__ mean) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  double acc = 0.0;
+  for (int64_t b = 0; b < nblk; ++b) acc += part[b * n + r];
+  mean[r] = (float)(acc / (double)N);
+}
+
+__global__ void sub_row_mean_kernel(float* __restrict__ X, int n, int64_t N,
+                                    const float* __restrict__ mean) {
+  const int64_t total = (int64_t)n * N;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x)
+    X[e] -= mean[e % n];
+}
+
 cudaError_t launch_advance_counter(int* ctr, cudaStream_t st) {
   advance_counter_kernel<<<1, 1, 0, st>>>(ctr);
+  return cudaGetLastError();
+}
+
+int64_t row_mean_blocks(int64_t N) { return (N + kRowChunk - 1) / kRowChunk; }
+
+cudaError_t launch_remove_row_mean(float* X, int n, int64_t N, double* part, float* mean,
+                                   cudaStream_t st) {
+  if (N <= 0) return cudaSuccess;
+  const int64_t nb = row_mean_blocks(N);
+  if (nb > 0x7fffffffLL) return cudaErrorInvalidValue;
+  row_partial_kernel<<<(unsigned)nb, 256, 0, st>>>(X, n, N, part);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  row_mean_kernel<<<(n + 255) / 256, 256, 0, st>>>(part, nb, n, N, mean);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  sub_row_mean_kernel<<<1216, 256, 0, st>>>(X, n, N, mean);
   return cudaGetLastError();
 }
 

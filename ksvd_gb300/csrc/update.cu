@@ -26,6 +26,7 @@ namespace {
 constexpr int kSigPerBlock = 256;      // signals per list-building block
 constexpr int kPrepThreads = 512;
 constexpr int kSweepThreads = 512;
+constexpr int kStageCap = 2048;   // list entries of the next atom staged per CTA (x2 buffers)
 constexpr unsigned kBarrierSpinLimit = 1u << 24;   // x >= 64 ns sleeps: > 1 s before giving up
 
 // ---- 1. atom lists --------------------------------------------------------------------------
@@ -339,6 +340,7 @@ struct Sweep {
   float* aD_s;     // Kp    a(j)'D
   float* cpart;    // Kp    this CTA's part of the new row j of C
   float* v_s;      // Kp    C(:, j') for the next atom (its left-out entry 0)
+  int32_t* stage;  // 2 x kStageCap: this CTA's list entries of the current / next atom
   float* red_f;
   int* red_i;
   int* sflag;
@@ -350,6 +352,7 @@ struct Sweep {
     aD_s = a_s + A.n;
     cpart = aD_s + A.Kp;
     v_s = cpart + A.Kp;
+    stage = reinterpret_cast<int32_t*>(v_s + A.Kp);
     tid = threadIdx.x;
     lane = tid & 31;
     w = tid >> 5;
@@ -491,15 +494,20 @@ struct Sweep {
     return anorm;
   }
 
-  // Issue L2 prefetches of the signals (and their codes) the next atom will read.
-  __device__ void prefetch_next(int jn, int gt, int gsize) {
+  // Stage this CTA's list entries of the next atom in shared memory (buffer `buf`) and issue L2
+  // prefetches of their signals and codes, so the next phase's loads start without a
+  // dependent list read and hit L2.
+  __device__ void prefetch_next(int jn, int buf, int gt, int gsize) {
     const int64_t q0 = A.start[jn], cnt = A.start[jn + 1] - q0;
     if (cnt == 0) return;
     const int64_t per = (cnt + nctas - 1) / nctas;
     const int64_t qa = q0 + min(cnt, (int64_t)c * per), qb = q0 + min(cnt, (int64_t)(c + 1) * per);
     const bool bulk_x = (A.n & 3) == 0, bulk_c = (A.T & 3) == 0;
+    int32_t* st = stage + buf * kStageCap;
     for (int64_t q = qa + gt; q < qb; q += gsize) {
-      const int64_t s = A.list[q] / A.T;
+      const int32_t e = A.list[q];
+      if (q - qa < kStageCap) st[q - qa] = e;
+      const int64_t s = e / A.T;
       const float* x = A.X + s * A.n;
       if (bulk_x) prefetch_l2_bulk(x, (uint32_t)A.n * 4);
       if (bulk_c) {
@@ -511,23 +519,24 @@ struct Sweep {
 
   // New coefficients of atom j for this CTA's share of its signals, by warps [0, gnw).  Adds
   // into cpart (C row j) and *use_cnt; the caller synchronises and flushes.
-  __device__ void update_coefs(int j, int64_t q0, int64_t cnt, float anorm, int gw, int gnw,
-                               int* use_cnt) {
+  __device__ void update_coefs(int j, int64_t q0, int64_t cnt, float anorm, int buf, int gw,
+                               int gnw, int* use_cnt) {
     const int n = A.n, K = A.K, T = A.T;
     const float aDj = aD_s[j];
     const int64_t per = (cnt + nctas - 1) / nctas;
     const int64_t qa = q0 + min(cnt, (int64_t)c * per), qb = q0 + min(cnt, (int64_t)(c + 1) * per);
+    const int32_t* st = stage + buf * kStageCap;
     int my_use = 0;
     for (int64_t qs = qa + (int64_t)gw * EB; qs < qb; qs += (int64_t)gnw * EB) {
       const int ne = (int)min((int64_t)EB, qb - qs);
       int64_t e[EB], s[EB];
-      int nz[EB];
 #pragma unroll
       for (int b = 0; b < EB; ++b) {
-        e[b] = b < ne ? A.list[qs + b] : 0;
+        const int64_t q = qs + b;
+        e[b] = b < ne ? (q - qa < kStageCap ? (int64_t)st[q - qa] : (int64_t)A.list[q]) : 0;
         s[b] = e[b] / T;
-        nz[b] = b < ne ? min(A.nnz[s[b]], T) : 0;
       }
+      // the signal, its whole code row and its support size, all in one round of loads
       float xv[EB][NPL];
 #pragma unroll
       for (int b = 0; b < EB; ++b)
@@ -537,17 +546,30 @@ struct Sweep {
           xv[b][i] = (b < ne && r < n) ? __ldcg(A.X + s[b] * n + r) : 0.f;
         }
       float cf[EB][2];
-      int ix[EB][2];
+      int ix[EB][2], nz[EB];
 #pragma unroll
-      for (int b = 0; b < EB; ++b)
+      for (int b = 0; b < EB; ++b) {
+        nz[b] = b < ne ? A.nnz[s[b]] : 0;
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
           const int t = lane + 32 * u;
-          const bool ok = t < nz[b];
-          const int v = ok ? A.idx[s[b] * T + t] : -1;
-          ix[b][u] = (v >= 0 && v < K) ? v : -1;
-          cf[b][u] = ok ? __ldcg(A.coef + s[b] * T + t) : 0.f;
+          const bool in = b < ne && t < T;
+          ix[b][u] = in ? A.idx[s[b] * T + t] : -1;
+          cf[b][u] = in ? __ldcg(A.coef + s[b] * T + t) : 0.f;
         }
+      }
+#pragma unroll
+      for (int b = 0; b < EB; ++b) {
+        const int lim = min(nz[b], T);
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const int t = lane + 32 * u;
+          const int v = ix[b][u];
+          const bool ok = t < lim && v >= 0 && v < K;
+          ix[b][u] = ok ? v : -1;
+          cf[b][u] = ok ? cf[b][u] : 0.f;
+        }
+      }
       float ax[EB], gs[EB];
 #pragma unroll
       for (int b = 0; b < EB; ++b) {
@@ -573,8 +595,11 @@ struct Sweep {
         }
 #pragma unroll
       for (int b = 0; b < EB; ++b) {
+        // gamma_j(s) is slot e % T of the code row already in registers
+        const int ts = (int)(e[b] - s[b] * T);
+        const float gold =
+            __shfl_sync(KSVD_FULL_MASK, (ts >> 5) == 0 ? cf[b][0] : cf[b][1], ts & 31);
         if (b >= ne) continue;
-        const float gold = __ldcg(A.coef + e[b]);
         const float g = (ax[b] - gs[b] + aDj * gold) / anorm;
 #pragma unroll
         for (int u = 0; u < 2; ++u)
@@ -691,7 +716,7 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
     __syncthreads();
     S.next_partials(j0, -1, A.avec, A.aDbuf, tid, blockDim.x);
     S.zero_row(j0, tid, blockDim.x);
-    S.prefetch_next(j0, tid, blockDim.x);
+    S.prefetch_next(j0, 0, tid, blockDim.x);
     if (!S.barrier()) return;
   }
   for (int jj = 0; jj < K; ++jj) {
@@ -711,11 +736,11 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
       if (jn >= 0) {
         S.next_partials(jn, j, av_next, ad_next, tid, blockDim.x);
         S.zero_row(jn, tid, blockDim.x);
-        S.prefetch_next(jn, tid, blockDim.x);
+        S.prefetch_next(jn, (jj + 1) & 1, tid, blockDim.x);
       }
     } else if (tid < HALF) {
       // warps 0..7: atom j's new coefficients
-      S.update_coefs(j, q0, cnt, anorm, tid >> 5, HALF >> 5, &use_cnt);
+      S.update_coefs(j, q0, cnt, anorm, jj & 1, tid >> 5, HALF >> 5, &use_cnt);
     } else {
       // warps 8..15: d_j, G/P rows of j, the next atom's partials, prefetch
       const int gt = tid - HALF;
@@ -725,7 +750,7 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
       if (jn >= 0) {
         S.next_partials(jn, j, av_next, ad_next, gt, HALF);
         S.zero_row(jn, gt, HALF);
-        S.prefetch_next(jn, gt, HALF);
+        S.prefetch_next(jn, (jj + 1) & 1, gt, HALF);
       }
     }
     __syncthreads();
@@ -794,7 +819,8 @@ cudaError_t launch_update_sweep(const UpdateArgs& a, cudaStream_t st) {
   s.avec = a.avec; s.aDbuf = a.aD; s.part = a.part; s.unused = a.unused; s.bitmap = a.bitmap;
   s.replaced = a.replaced; s.counter = a.counter; s.usecount = a.usecount; s.barrier = a.barrier;
   s.dev_err = a.dev_err;
-  const size_t smem = sizeof(float) * ((size_t)a.n + 3 * (size_t)a.Kp);
+  const size_t smem = sizeof(float) * ((size_t)a.n + 3 * (size_t)a.Kp) +
+                      sizeof(int32_t) * 2 * kStageCap;
   const int npl = (a.n + 31) / 32;
   auto launch = [&](auto kern) -> cudaError_t {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
