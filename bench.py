@@ -273,6 +273,7 @@ def run_batched(args):
         cpu = cpu_baseline_batched(probs, max(200, args.cpu_sample // 64))
     Ntot = sum(q["N"] for q in probs)
     h = Handle(1, 1, 1, profile=True)
+    tuning = h.autotune_batched(probs)
     outs, _ = h.batched_iterate(probs, args.warmup)
     torch.cuda.synchronize()
     h.stage_times(reset=True)
@@ -330,7 +331,7 @@ def run_batched(args):
                    " error-constrained OMP, one K-SVD iteration of every problem per step"
                    % (len(probs), Ntot), "problems": len(probs), "signals": Ntot,
                    "l2": "inputs larger than L2 (X = %.2f GB)"
-                   % (sum(q["X"].numel() for q in probs) * 4 / 1e9)},
+                   % (sum(q["X"].numel() for q in probs) * 4 / 1e9), "autotuned": tuning},
         "omp_signals_per_s": {"value": Ntot / ((omp_ms + gemm_ms) / 1e3), "unit": "signals/s",
                               "stages": "grouped D'X/Gram GEMM + persistent batched OMP",
                               "omp_ms": omp_ms, "gemm_ms": gemm_ms},
@@ -344,6 +345,69 @@ def run_batched(args):
     print(json.dumps(line), flush=True)
     h.close()
     return 0
+
+
+def run_adjoint(args):
+    """Fixed-support coding forward + adjoint backward (n=128, K=512, N=100,000, T=12): one step
+    = ksvd_code_fixed then ksvd_code_backward on every signal; signals/s."""
+    import torch
+
+    from ksvd_gb300 import Handle, datagen
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    cfg = datagen.CONFIGS["cfg4"]
+    p = datagen.make_problem(cfg, N=args.signals, device="cuda")
+    X, D = p["X"], p["D"]
+    N = X.shape[0]
+    h = Handle(cfg.n, cfg.K, cfg.T)
+    idx, _, nnz = h.omp(D, X)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(7)
+    dcoef = torch.randn((N, cfg.T), generator=g, device="cuda")
+    dD = torch.zeros_like(D)
+    dX = torch.empty_like(X)
+    coef = torch.empty((N, cfg.T), dtype=torch.float32, device="cuda")
+    chol = torch.empty((N, cfg.T * (cfg.T + 1) // 2), dtype=torch.float32, device="cuda")
+
+    def step():
+        h._check(h._lib.ksvd_code_fixed(h._h, _p(D), _p(X), N, _p(idx), _p(nnz), _p(coef),
+                                        _p(chol)))
+        dD.zero_()
+        h._check(h._lib.ksvd_code_backward(h._h, _p(D), _p(X), N, _p(idx), _p(nnz), _p(coef),
+                                           _p(chol), _p(dcoef), _p(dD), _p(dX)))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    # per signal: x read twice, t support columns gathered three times (L2), chol, code and
+    # gradients written
+    t = cfg.T
+    byts = N * (2 * cfg.n * 4 + t * (t + 1) // 2 * 8 + t * 12 + cfg.n * 4 + 8)
+    pk = peaks()
+    line = {"metric": "adjoint_signals_per_s", "value": N / (ms / 1e3), "unit": "signals/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "dtype": "fp32", "data": "synthetic (seeded, cfg4 shape)",
+            "config": {"workload": "cfg4: n=128 K=512 N=%d T=12, forward + backward" % N},
+            "roofline": {"bound": "hbm", "achieved": byts / (ms / 1e3) / 1e9, "peak": pk["hbm"],
+                         "unit": "GB/s", "frac": byts / (ms / 1e3) / 1e9 / pk["hbm"]}}
+    print(json.dumps(line), flush=True)
+    h.close()
+    return 0
+
+
+def _p(t):
+    import ctypes
+
+    return ctypes.c_void_p(t.data_ptr())
 
 
 def main():
@@ -368,6 +432,8 @@ def main():
 
     if args.config == "cfg3":
         return run_reference(args, None) if args.impl == "reference" else run_batched(args)
+    if args.config == "cfg4" and args.impl != "reference":
+        return run_adjoint(args)
     cfg = datagen.CONFIGS[args.config]
     if args.signals:
         import dataclasses
@@ -404,6 +470,8 @@ def main():
     # a second, profiling handle measures per-stage times (events) in a separate pass
     h = Handle(cfg.n, cfg.K, cfg.T, precision=args.precision, graph=not args.no_graph)
     hp = Handle(cfg.n, cfg.K, cfg.T, precision=args.precision, profile=True)
+    tuning = h.autotune(D, X)                     # launch shapes timed on this workload
+    hp.tuning = tuning
     idx, coef, nnz = h._code(N, dev)
     out = (idx, coef, nnz)
     rms = list(h.iterate(D, X, args.warmup, out=out)[3])
@@ -505,6 +573,7 @@ def main():
                        "parallelism": "replicas%d" % ws if ws > 1 else "single",
                        "cuda_graph": {"enabled": not args.no_graph,
                                       "replayed_iterations": replays},
+                       "autotuned": tuning,
                        "l2": "inputs larger than L2 (X = %.2f GB)" % (X.numel() * 4 / 1e9)},
             "omp_signals_per_s": {"value": ws * N / (omp_ms / 1e3) if omp_ms else None,
                                   "unit": "signals/s", "stages": "D'X + Batch-OMP"},

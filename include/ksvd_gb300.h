@@ -219,6 +219,32 @@ KSVD_API ksvd_status ksvd_code_backward(ksvd_handle* handle, const float* D, con
  * flag is off or capture was refused, in which case the iterations ran as plain launches). */
 KSVD_API int64_t ksvd_graph_replays(const ksvd_handle* handle);
 
+/* ---- autotuning --------------------------------------------------------------------------- */
+
+/* Launch shapes chosen per handle (0 = the built-in default). */
+typedef struct ksvd_tuning {
+  int32_t omp_grid_mult; /* Batch-OMP blocks = resident CTA slots x this (grid-stride)          */
+  int32_t sweep_ctas;    /* CTAs of the cooperative atom sweep (0: one per SM)                  */
+  int32_t batch_chunk;   /* signals per work-queue chunk of the batched Batch-OMP (default 16)  */
+  int32_t batch_concurrent; /* ksvd_batched_iterate: 1 = per-problem updates concurrently on
+                               their own streams with SM shares; 0 (default) = one after
+                               another, each sweep on the whole GPU                            */
+  int32_t tuned;         /* 1 after an autotune call                                           */
+} ksvd_tuning;
+
+/* Times Batch-OMP grid sizes and sweep CTA counts on this problem (D n x K, X n x N, device) and
+ * keeps the fastest for the handle's later calls; D, X and the atom-order stream are not
+ * changed.  Costs a few OMP and dictionary-update passes.  No reference counterpart. */
+KSVD_API ksvd_status ksvd_autotune(ksvd_handle* handle, const float* D, const float* X, int64_t N,
+                                   ksvd_tuning* out);
+/* Times the batched work-queue chunk (ksvd_batched_omp) and the batched update mode (one
+ * iteration of ksvd_batched_iterate; the dictionaries are restored afterwards) on these
+ * problems. */
+KSVD_API ksvd_status ksvd_autotune_batched(ksvd_handle* handle, const struct ksvd_problem* probs,
+                                           int32_t nprob, ksvd_tuning* out);
+KSVD_API ksvd_status ksvd_get_tuning(const ksvd_handle* handle, ksvd_tuning* out);
+KSVD_API ksvd_status ksvd_set_tuning(ksvd_handle* handle, const ksvd_tuning* tuning);
+
 /* ---- many independent problems ------------------------------------------------------------- */
 
 /* One problem of a batched call.  Device pointers, column-major like the single-problem calls. */
@@ -246,8 +272,9 @@ KSVD_API ksvd_status ksvd_batched_omp(ksvd_handle* handle, const ksvd_problem* p
 
 /* iters K-SVD iterations of every problem (each N >= 1): per iteration ONE persistent Batch-OMP
  * launch over all problems (as ksvd_batched_omp), then every problem's dictionary update, error
- * and clearDict concurrently on its own stream (the cooperative sweeps share the SMs in
- * proportion to N*T).  D is normalised first and updated in place; idx/coef/nnz hold the last
+ * and clearDict -- one after another with each sweep on the whole GPU, or (tuning
+ * batch_concurrent) concurrently on their own streams with the cooperative sweeps sharing the
+ * SMs in proportion to N*T.  D is normalised first and updated in place; idx/coef/nnz hold the last
  * iteration's code; rmse (host, nullable) gets nprob x iters values, problem-major.  The
  * handle's mu_thresh, use_thresh, max_replace_signals and seed apply to every problem (FP32).
  * Replaces a host loop of KSVD::ExecuteIterations calls (S/KSVD.cu:55-131), one per dictionary. */

@@ -33,6 +33,7 @@ EXPORTS = (
     "ksvd_rmse_noalloc", "ksvd_code_fixed", "ksvd_code_backward",
     "ksvd_refine_coefs", "ksvd_batched_omp", "ksvd_graph_replays",
     "ksvd_batched_iterate", "ksvd_remove_row_mean", "ksvd_perm_draws", "ksvd_set_perm_draws",
+    "ksvd_autotune", "ksvd_autotune_batched", "ksvd_get_tuning", "ksvd_set_tuning",
 )
 
 FLAG_PROFILE = 1
@@ -51,6 +52,16 @@ class Params(C.Structure):
         ("mu_thresh", C.c_float), ("use_thresh", C.c_int32),
         ("max_replace_signals", C.c_int32), ("flags", C.c_int32), ("seed", C.c_uint64),
     ]
+
+
+class Tuning(C.Structure):
+    """ksvd_tuning: launch shapes chosen per handle."""
+    _fields_ = [("omp_grid_mult", C.c_int32), ("sweep_ctas", C.c_int32),
+                ("batch_chunk", C.c_int32), ("batch_concurrent", C.c_int32),
+                ("tuned", C.c_int32)]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
 
 
 class Problem(C.Structure):
@@ -109,6 +120,10 @@ def _declare(lib):
         "ksvd_remove_row_mean": (st, [vp, vp, i64, vp]),
         "ksvd_perm_draws": (i64, [vp]),
         "ksvd_set_perm_draws": (st, [vp, i64]),
+        "ksvd_autotune": (st, [vp, vp, vp, i64, vp]),
+        "ksvd_autotune_batched": (st, [vp, vp, i32, vp]),
+        "ksvd_get_tuning": (st, [vp, vp]),
+        "ksvd_set_tuning": (st, [vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -130,6 +130,29 @@ class Handle:
     def perm_draws(self, v):
         self._check(self._lib.ksvd_set_perm_draws(self._h, int(v)))
 
+    def autotune(self, D, X):
+        """Time launch shapes on this problem and keep the fastest; returns the choice."""
+        t = _native.Tuning()
+        self._check(self._lib.ksvd_autotune(self._h, _ptr(D), _ptr(X), X.shape[0], C.byref(t)))
+        return t.as_dict()
+
+    def autotune_batched(self, problems):
+        arr, _ = self._problems(problems)
+        t = _native.Tuning()
+        self._check(self._lib.ksvd_autotune_batched(self._h, arr, len(problems), C.byref(t)))
+        return t.as_dict()
+
+    @property
+    def tuning(self):
+        t = _native.Tuning()
+        self._check(self._lib.ksvd_get_tuning(self._h, C.byref(t)))
+        return t.as_dict()
+
+    @tuning.setter
+    def tuning(self, d):
+        t = _native.Tuning(**{k: int(v) for k, v in d.items()})
+        self._check(self._lib.ksvd_set_tuning(self._h, C.byref(t)))
+
     def graph_replays(self) -> int:
         """Iterations ksvd_iterate ran as CUDA-graph replays on this handle."""
         return int(self._lib.ksvd_graph_replays(self._h))

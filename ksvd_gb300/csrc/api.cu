@@ -66,6 +66,11 @@ struct ksvd_handle {
   std::vector<cudaEvent_t> kid_events;
   cudaEvent_t fork_ev = nullptr;
   int sweep_ctas = 0;   // CTAs of this handle's cooperative sweep (0: one per SM)
+  int omp_grid_mult = 0;  // Batch-OMP blocks per resident CTA slot (0: default)
+  int batch_chunk = 0;    // signals per batched work-queue chunk (0: default)
+  int batch_concurrent = 0;  // batched updates: 1 = concurrent streams with SM shares,
+                             // 0 = one after another, each sweep on the whole GPU
+  bool tuned = false;
   // host copies of the batched call's tables (kept alive for the asynchronous uploads)
   std::vector<ksvd::GemmDesc> batch_descs;
   std::vector<ksvd::OmpJob> batch_jobs;
@@ -77,7 +82,7 @@ enum BufId {
   B_DPAD, B_G, B_A0, B_XN2, B_LIST, B_START, B_BHIST, B_Y, B_GN2, B_C, B_AVEC, B_AD, B_PART,
   B_UNUSED, B_BITMAP, B_REPLACED, B_COUNTER, B_USE, B_BARRIER, B_ERR, B_PSUM, B_BVAL, B_BIDX,
   B_RMSE, B_M, B_MI, B_CLEARED, B_DEVERR, B_PERM, B_GPAD_IN, B_HX, B_HD, B_HIDX, B_HCOEF, B_HNNZ,
-  B_XHI, B_XLO, B_DHI, B_DLO, B_P, B_BG, B_BA0, B_BDESC, B_BJOB, B_BQUEUE, B_ITER, B_RPART, B_RMEAN, B_COUNT
+  B_XHI, B_XLO, B_DHI, B_DLO, B_P, B_BG, B_BA0, B_BDESC, B_BJOB, B_BQUEUE, B_ITER, B_RPART, B_RMEAN, B_TUNE_D, B_TUNE_C, B_COUNT
 };
 
 ksvd_status fail(ksvd_handle* h, ksvd_status s, const char* fmt, const char* detail = nullptr) {
@@ -290,7 +295,7 @@ ksvd_status run_omp(ksvd_handle* h, const float* G, const float* A0, int64_t N,
   KSVD_TRY(ensure(h, B_DEVERR, 1, &de));
   StageScope sc(h, KSVD_STAGE_OMP);
   KSVD_CK(h, launch_omp(G, h->Kp, A0, h->Kp, h->p.K, N, h->p.T, xnorm2, eps2, idx, coef, nnz, de,
-                        h->stream));
+                        h->stream, h->omp_grid_mult));
   return KSVD_OK;
 }
 
@@ -716,7 +721,7 @@ ksvd_status ksvd_batched_omp(ksvd_handle* h, const ksvd_problem* probs, int32_t 
   jobs.assign((size_t)nprob, OmpJob{});
   int64_t tiles = 0, chunks = 0;
   int nd = 0, nj = 0;
-  const int chunk = omp_batch_chunk();
+  const int chunk = h->batch_chunk > 0 ? h->batch_chunk : omp_batch_chunk();
   for (int32_t i = 0; i < nprob; ++i) {
     const ksvd_problem& q = probs[i];
     if (q.N == 0) continue;
@@ -742,7 +747,7 @@ ksvd_status ksvd_batched_omp(ksvd_handle* h, const ksvd_problem* probs, int32_t 
     KSVD_CK(h, launch_gemm_tn_f32_grouped(ddev, nd, tiles, h->stream));
   }
   StageScope sc(h, KSVD_STAGE_OMP);
-  KSVD_CK(h, launch_omp_batched(jdev, nj, chunks, tmax, queue, de, h->stream));
+  KSVD_CK(h, launch_omp_batched(jdev, nj, chunks, tmax, chunk, queue, de, h->stream));
   return KSVD_OK;
 }
 
@@ -823,12 +828,14 @@ ksvd_status ksvd_batched_iterate(ksvd_handle* h, ksvd_problem* probs, int32_t np
   std::vector<double*> rd(nprob);
   std::vector<int32_t*> cd(nprob);
   std::vector<ksvd_problem> inner(probs, probs + nprob);
+  const bool conc = h->batch_concurrent != 0;
   int budget = sms - nprob;   // every problem has one CTA; the rest go by work
   for (int32_t i = 0; i < nprob; ++i) {
     KSVD_TRY(batch_child(h, i, probs[i], &ks[i]));
     ksvd_handle* k = ks[i];
     const int extra = budget > 0 ? (int)((double)budget * probs[i].N * probs[i].T / work) : 0;
-    k->sweep_ctas = std::max(1, 1 + extra);
+    // concurrent: shares that fit on the GPU together; sequential: every sweep gets all SMs
+    k->sweep_ctas = conc ? std::max(1, 1 + extra) : 0;
   }
   KSVD_TRY(batch_fork(h, nprob));
   for (int32_t i = 0; i < nprob; ++i) {
@@ -845,19 +852,24 @@ ksvd_status ksvd_batched_iterate(ksvd_handle* h, ksvd_problem* probs, int32_t np
   KSVD_TRY(batch_join(h, nprob));
   for (int32_t it = 0; it < iters; ++it) {
     KSVD_TRY(ksvd_batched_omp(h, inner.data(), nprob));
-    KSVD_TRY(batch_fork(h, nprob));
+    if (conc) KSVD_TRY(batch_fork(h, nprob));
     for (int32_t i = 0; i < nprob; ++i) {
       ksvd_handle* k = ks[i];
       const ksvd_problem& q = probs[i];
+      // sequential mode runs every problem's stages on the parent stream, in order
+      const cudaStream_t own = k->stream;
+      if (!conc) k->stream = h->stream;
       float* G = nullptr;
-      KSVD_TRY(kid_error(h, k, ensure(k, B_G, (size_t)k->Kp * k->Kp, &G)));
-      KSVD_TRY(kid_error(h, k, run_update(k, Dp[i], q.X, q.N, q.idx, q.coef, q.nnz,
-                                          pd[i] + (size_t)it * q.K)));
-      KSVD_TRY(kid_error(h, k, run_error(k, Dp[i], q.X, q.N, q.idx, q.coef, q.nnz, rd[i] + it)));
-      KSVD_TRY(kid_error(h, k, gram_padded(k, Dp[i], G)));
-      KSVD_TRY(kid_error(h, k, run_clear(k, Dp[i], G, q.X, q.N, cd[i])));
+      ksvd_status s2 = ensure(k, B_G, (size_t)k->Kp * k->Kp, &G);
+      if (s2 == KSVD_OK)
+        s2 = run_update(k, Dp[i], q.X, q.N, q.idx, q.coef, q.nnz, pd[i] + (size_t)it * q.K);
+      if (s2 == KSVD_OK) s2 = run_error(k, Dp[i], q.X, q.N, q.idx, q.coef, q.nnz, rd[i] + it);
+      if (s2 == KSVD_OK) s2 = gram_padded(k, Dp[i], G);
+      if (s2 == KSVD_OK) s2 = run_clear(k, Dp[i], G, q.X, q.N, cd[i]);
+      k->stream = own;
+      KSVD_TRY(kid_error(h, k, s2));
     }
-    KSVD_TRY(batch_join(h, nprob));
+    if (conc) KSVD_TRY(batch_join(h, nprob));
   }
   KSVD_TRY(batch_fork(h, nprob));
   for (int32_t i = 0; i < nprob; ++i) {
@@ -870,6 +882,211 @@ ksvd_status ksvd_batched_iterate(ksvd_handle* h, ksvd_problem* probs, int32_t np
   KSVD_CK(h, cudaStreamSynchronize(h->stream));
   for (int32_t i = 0; i < nprob; ++i) KSVD_TRY(kid_error(h, ks[i], check_dev_err(ks[i])));
   return check_dev_err(h);
+}
+
+}  // extern "C"
+
+namespace {
+
+// Median of `reps` timings (ms) of fn() on the handle's stream, after one untimed run.
+template <typename F>
+ksvd_status time_on_stream(ksvd_handle* h, int reps, F fn, double* ms_out) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  KSVD_CK(h, cudaEventCreate(&a));
+  KSVD_CK(h, cudaEventCreate(&b));
+  std::vector<float> t;
+  ksvd_status st = fn();
+  for (int r = 0; r < reps && st == KSVD_OK; ++r) {
+    cudaEventRecord(a, h->stream);
+    st = fn();
+    cudaEventRecord(b, h->stream);
+    float ms = 0.f;
+    if (st == KSVD_OK && cudaEventSynchronize(b) == cudaSuccess &&
+        cudaEventElapsedTime(&ms, a, b) == cudaSuccess)
+      t.push_back(ms);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (st != KSVD_OK) return st;
+  if (t.empty()) return fail(h, KSVD_ERR_CUDA, "autotune timing failed%s");
+  std::sort(t.begin(), t.end());
+  *ms_out = t[t.size() / 2];
+  return KSVD_OK;
+}
+
+void fill_tuning(const ksvd_handle* h, ksvd_tuning* out) {
+  if (!out) return;
+  std::memset(out, 0, sizeof(*out));
+  out->omp_grid_mult = h->omp_grid_mult;
+  out->sweep_ctas = h->sweep_ctas;
+  out->batch_chunk = h->batch_chunk;
+  out->batch_concurrent = h->batch_concurrent;
+  out->tuned = h->tuned ? 1 : 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Times the launch shapes that have no single best value across problem sizes on this GPU and
+// this problem, and keeps the fastest for the handle's later calls:
+//   * Batch-OMP grid: resident CTA slots x {1, 2, 4, 8, 16} blocks (grid-stride over signals);
+//   * the cooperative sweep's CTAs: {SMs, SMs/2, SMs/4} (fewer CTAs make the per-atom grid
+//     barrier cheaper, more spread each atom's signals wider).
+// The inputs are not modified: the sweep runs on scratch copies of D and the coefficients, and
+// the handle's atom-order stream and stage state are restored.
+ksvd_status ksvd_autotune(ksvd_handle* h, const float* D, const float* X, int64_t N,
+                          ksvd_tuning* out) {
+  if (!h || bad_ptr(D) || bad_ptr(X) || N < 1) return KSVD_ERR_INVALID_ARGUMENT;
+  if ((int64_t)N * h->p.T > 0x7fffffffLL)
+    return fail(h, KSVD_ERR_UNSUPPORTED, "N*T must stay below 2^31%s");
+  const int n = h->p.n, Kp = h->Kp, T = h->p.T;
+  drop_xsplit(h);
+  float *Dp = nullptr, *G = nullptr, *A0 = nullptr, *Dt = nullptr, *Ct = nullptr, *coef = nullptr;
+  int32_t *idx = nullptr, *nnz = nullptr, *pd = nullptr;
+  KSVD_TRY(load_dict(h, D, &Dp));
+  KSVD_CK(h, launch_normcols(Dp, n, h->p.K, h->stream));
+  KSVD_TRY(ensure(h, B_G, (size_t)Kp * Kp, &G));
+  KSVD_TRY(ensure(h, B_A0, (size_t)Kp * N, &A0));
+  KSVD_TRY(ensure(h, B_HIDX, (size_t)N * T, &idx));
+  KSVD_TRY(ensure(h, B_HCOEF, (size_t)N * T, &coef));
+  KSVD_TRY(ensure(h, B_HNNZ, (size_t)N, &nnz));
+  KSVD_TRY(ensure(h, B_TUNE_D, (size_t)n * Kp, &Dt));
+  KSVD_TRY(ensure(h, B_TUNE_C, (size_t)N * T, &Ct));
+  KSVD_TRY(gram_padded(h, Dp, G));
+  KSVD_TRY(dtx_padded(h, Dp, X, N, A0));
+  const bool prof = h->profiling();
+  h->p.flags &= ~KSVD_FLAG_PROFILE;        // no stage events while tuning
+  ksvd_status st = KSVD_OK;
+  double best = 1e30;
+  int best_mult = 8;
+  for (int mult : {1, 2, 4, 8, 16}) {
+    h->omp_grid_mult = mult;
+    double ms = 0;
+    st = time_on_stream(h, 3, [&] {
+      return run_omp(h, G, A0, N, nullptr, nullptr, idx, coef, nnz);
+    }, &ms);
+    if (st != KSVD_OK) break;
+    if (ms < best) { best = ms; best_mult = mult; }
+  }
+  h->omp_grid_mult = best_mult;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+  const int64_t draws = h->perm_draws;
+  if (st == KSVD_OK) st = upload_perm(h, nullptr, 1, &pd);
+  best = 1e30;
+  int best_ctas = 0;
+  for (int div : {1, 2, 4}) {
+    if (st != KSVD_OK) break;
+    const int ctas = std::max(1, sms / div);
+    h->sweep_ctas = ctas;
+    double ms = 0;
+    st = time_on_stream(h, 2, [&]() -> ksvd_status {
+      KSVD_CK(h, cudaMemcpyAsync(Dt, Dp, sizeof(float) * (size_t)n * Kp,
+                                 cudaMemcpyDeviceToDevice, h->stream));
+      KSVD_CK(h, cudaMemcpyAsync(Ct, coef, sizeof(float) * (size_t)N * T,
+                                 cudaMemcpyDeviceToDevice, h->stream));
+      return run_update(h, Dt, X, N, idx, Ct, nnz, pd);
+    }, &ms);
+    if (st == KSVD_OK && ms < best) { best = ms; best_ctas = div == 1 ? 0 : ctas; }
+  }
+  h->sweep_ctas = best_ctas;
+  h->perm_draws = draws;
+  h->update_N = -1;
+  h->error_N = -1;
+  if (prof) h->p.flags |= KSVD_FLAG_PROFILE;
+  drop_xsplit(h);
+  if (st != KSVD_OK) return st;
+  KSVD_CK(h, cudaStreamSynchronize(h->stream));
+  KSVD_TRY(check_dev_err(h));
+  h->tuned = true;
+  fill_tuning(h, out);
+  return KSVD_OK;
+}
+
+// Work-queue chunk of the batched Batch-OMP ({4, 16, 64} signals) and the batched update mode,
+// timed on the given problems.
+ksvd_status ksvd_autotune_batched(ksvd_handle* h, const ksvd_problem* probs, int32_t nprob,
+                                  ksvd_tuning* out) {
+  if (!h || nprob < 1 || !probs) return KSVD_ERR_INVALID_ARGUMENT;
+  const bool prof = h->profiling();
+  h->p.flags &= ~KSVD_FLAG_PROFILE;
+  ksvd_status st = KSVD_OK;
+  double best = 1e30;
+  int best_chunk = 16;
+  for (int chunk : {4, 16, 64}) {
+    h->batch_chunk = chunk;
+    double ms = 0;
+    st = time_on_stream(h, 2, [&] { return ksvd_batched_omp(h, probs, nprob); }, &ms);
+    if (st != KSVD_OK) break;
+    if (ms < best) { best = ms; best_chunk = chunk; }
+  }
+  h->batch_chunk = best_chunk;
+  // updates: concurrent streams with SM shares vs one after another on the whole GPU, timed
+  // on one K-SVD iteration; the dictionaries and the children's atom-order streams are restored
+  std::vector<float*> saved(nprob, nullptr);
+  std::vector<ksvd_problem> work(probs, probs + nprob);
+  bool all_n = true;
+  for (int32_t i = 0; i < nprob; ++i) all_n &= probs[i].N >= 1;
+  for (int32_t i = 0; i < nprob && st == KSVD_OK && all_n; ++i) {
+    const size_t bytes = sizeof(float) * (size_t)probs[i].n * probs[i].K;
+    if (cudaMalloc(&saved[i], bytes) != cudaSuccess ||
+        cudaMemcpyAsync(saved[i], probs[i].D, bytes, cudaMemcpyDeviceToDevice, h->stream) !=
+            cudaSuccess)
+      st = cuda_fail(h, cudaGetLastError(), "autotune scratch");
+  }
+  if (st == KSVD_OK && all_n) {
+    std::vector<int64_t> draws;
+    for (auto k : h->kids) draws.push_back(k ? k->perm_draws : 0);
+    best = 1e30;
+    int best_mode = 0;
+    for (int mode : {0, 1}) {
+      h->batch_concurrent = mode;
+      double ms = 0;
+      st = time_on_stream(h, 1, [&]() -> ksvd_status {
+        for (int32_t i = 0; i < nprob; ++i)
+          KSVD_CK(h, cudaMemcpyAsync(work[i].D, saved[i],
+                                     sizeof(float) * (size_t)probs[i].n * probs[i].K,
+                                     cudaMemcpyDeviceToDevice, h->stream));
+        return ksvd_batched_iterate(h, work.data(), nprob, 1, nullptr);
+      }, &ms);
+      if (st != KSVD_OK) break;
+      if (ms < best) { best = ms; best_mode = mode; }
+    }
+    h->batch_concurrent = best_mode;
+    for (int32_t i = 0; i < nprob; ++i)
+      cudaMemcpyAsync(work[i].D, saved[i], sizeof(float) * (size_t)probs[i].n * probs[i].K,
+                      cudaMemcpyDeviceToDevice, h->stream);
+    for (size_t i = 0; i < h->kids.size(); ++i)
+      if (h->kids[i]) h->kids[i]->perm_draws = i < draws.size() ? draws[i] : 0;
+  }
+  cudaStreamSynchronize(h->stream);
+  for (auto p : saved)
+    if (p) cudaFree(p);
+  if (prof) h->p.flags |= KSVD_FLAG_PROFILE;
+  if (st != KSVD_OK) return st;
+  KSVD_TRY(check_dev_err(h));
+  h->tuned = true;
+  fill_tuning(h, out);
+  return KSVD_OK;
+}
+
+ksvd_status ksvd_get_tuning(const ksvd_handle* h, ksvd_tuning* out) {
+  if (!h || !out) return KSVD_ERR_INVALID_ARGUMENT;
+  fill_tuning(h, out);
+  return KSVD_OK;
+}
+
+ksvd_status ksvd_set_tuning(ksvd_handle* h, const ksvd_tuning* t) {
+  if (!h || !t || t->omp_grid_mult < 0 || t->omp_grid_mult > 64 || t->sweep_ctas < 0 ||
+      t->batch_chunk < 0 || t->batch_chunk > 4096)
+    return KSVD_ERR_INVALID_ARGUMENT;
+  h->omp_grid_mult = t->omp_grid_mult;
+  h->sweep_ctas = t->sweep_ctas;
+  h->batch_chunk = t->batch_chunk;
+  h->batch_concurrent = t->batch_concurrent != 0;
+  h->tuned = t->tuned != 0;
+  return KSVD_OK;
 }
 
 ksvd_status ksvd_update_dictionary(ksvd_handle* h, float* D, const float* X, int64_t N,

@@ -38,9 +38,11 @@ cudaError_t launch_split_bf16(const float* in, int64_t ld_in, int64_t rows, int 
 int omp_padded_k(int K);
 // G: Kp x Kp column-major (ldg >= Kp), zero padded; A0: Kp x N column-major (lda >= Kp), zero
 // padded, with Kp = omp_padded_k(K).  T <= 64.
+// grid_mult: resident CTAs per SM x grid_mult blocks at most (0 = default 8; the autotuner's knob)
 cudaError_t launch_omp(const float* G, int64_t ldg, const float* A0, int64_t lda, int K,
                        int64_t N, int T, const float* xnorm2, const float* eps2, int32_t* idx,
-                       float* coef, int32_t* nnz, int* dev_err, cudaStream_t st);
+                       float* coef, int32_t* nnz, int* dev_err, cudaStream_t st,
+                       int grid_mult = 0);
 
 // ---- misc (misc.cu) ---------------------------------------------------------------------------
 cudaError_t launch_normcols(float* D, int n, int K, cudaStream_t st);
@@ -149,10 +151,12 @@ struct OmpJob {
   int64_t N; int64_t chunk_begin;   // first work-queue chunk of this job
   int n, K, kpl, T;                 // kpl = Kp / 32 (4, 8, 16 or 32)
 };
-int omp_batch_chunk();              // signals per work-queue chunk
-// jobs_dev sorted by chunk_begin; tmax = max T over the jobs.  Zeroes *queue on the stream.
+int omp_batch_chunk();              // default signals per work-queue chunk
+// jobs_dev sorted by chunk_begin (chunk_begin in units of `chunk` signals); tmax = max T over
+// the jobs.  Zeroes *queue on the stream.
 cudaError_t launch_omp_batched(const OmpJob* jobs_dev, int njobs, int64_t total_chunks, int tmax,
-                               unsigned long long* queue, int* dev_err, cudaStream_t st);
+                               int chunk, unsigned long long* queue, int* dev_err,
+                               cudaStream_t st);
 
 // ---- grouped FP32 GEMM: many C = A'B products (different sizes) in one launch -------------------
 struct GemmDesc {

@@ -237,12 +237,12 @@ omp_kernel(const float* __restrict__ G, int64_t ldg, const float* __restrict__ A
 // atomicAdd on *queue (zeroed before the launch); chunk c belongs to the job whose range
 // [chunk_begin, chunk_begin + ceil(N / kChunk)) holds it.  In error-constrained jobs ||x||^2
 // comes from X in the same pass.
-constexpr int kBatchChunk = 16;
+constexpr int kBatchChunk = 16;   // default signals per work-queue chunk
 
 template <int TMAX>
 __global__ void __launch_bounds__(kOmpWarps * 32, (TMAX <= 32 ? 2 : 1))
 omp_batched_kernel(const OmpJob* __restrict__ jobs, int njobs, int64_t total_chunks,
-                   unsigned long long* __restrict__ queue, int* __restrict__ dev_err) {
+                   int chunk, unsigned long long* __restrict__ queue, int* __restrict__ dev_err) {
   constexpr int LS = TMAX + 1;
   extern __shared__ __align__(16) float smem[];
   const int lane = threadIdx.x & 31;
@@ -261,8 +261,8 @@ omp_batched_kernel(const OmpJob* __restrict__ jobs, int njobs, int64_t total_chu
       if (jobs[mid].chunk_begin <= (int64_t)c) lo = mid; else hi = mid - 1;
     }
     const OmpJob& jb = jobs[lo];
-    const int64_t s0 = ((int64_t)c - jb.chunk_begin) * kBatchChunk;
-    const int64_t s1 = min(jb.N, s0 + kBatchChunk);
+    const int64_t s0 = ((int64_t)c - jb.chunk_begin) * chunk;
+    const int64_t s1 = min(jb.N, s0 + chunk);
     const bool emode = jb.eps2 != nullptr;
     for (int64_t s = s0; s < s1; ++s) {
       float xn2 = 0.f, e2 = 0.f;
@@ -301,7 +301,8 @@ omp_batched_kernel(const OmpJob* __restrict__ jobs, int njobs, int64_t total_chu
 template <int KPL, int TMAX>
 cudaError_t launch_omp_t(const float* G, int64_t ldg, const float* A0, int64_t lda, int K,
                          int64_t N, int T, const float* xnorm2, const float* eps2, int32_t* idx,
-                         float* coef, int32_t* nnz, int* dev_err, cudaStream_t st) {
+                         float* coef, int32_t* nnz, int* dev_err, int grid_mult,
+                         cudaStream_t st) {
   const size_t smem = (size_t)kOmpWarps * (TMAX * (TMAX + 1) + 32 * KPL) * sizeof(float);
   auto kern = omp_kernel<KPL, TMAX>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -313,7 +314,7 @@ cudaError_t launch_omp_t(const float* G, int64_t ldg, const float* A0, int64_t l
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kOmpWarps * 32, smem);
   if (per_sm < 1) per_sm = 1;
   int64_t blocks = (N + kOmpWarps - 1) / kOmpWarps;
-  const int64_t cap = (int64_t)sms * per_sm * 8;
+  const int64_t cap = (int64_t)sms * per_sm * (grid_mult > 0 ? grid_mult : 8);
   if (blocks > cap) blocks = cap;
   kern<<<(unsigned)blocks, kOmpWarps * 32, smem, st>>>(G, ldg, A0, lda, K, N, T, xnorm2, eps2, idx,
                                                        coef, nnz, dev_err);
@@ -321,7 +322,7 @@ cudaError_t launch_omp_t(const float* G, int64_t ldg, const float* A0, int64_t l
 }
 
 template <int TMAX>
-cudaError_t launch_omp_batched_t(const OmpJob* jobs, int njobs, int64_t total_chunks,
+cudaError_t launch_omp_batched_t(const OmpJob* jobs, int njobs, int64_t total_chunks, int chunk,
                                  unsigned long long* queue, int* dev_err, cudaStream_t st) {
   const size_t smem = (size_t)kOmpWarps * (TMAX * (TMAX + 1) + 32 * 32) * sizeof(float);
   auto kern = omp_batched_kernel<TMAX>;
@@ -338,7 +339,8 @@ cudaError_t launch_omp_batched_t(const OmpJob* jobs, int njobs, int64_t total_ch
   if (blocks > need) blocks = need;
   e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
-  kern<<<(unsigned)blocks, kOmpWarps * 32, smem, st>>>(jobs, njobs, total_chunks, queue, dev_err);
+  kern<<<(unsigned)blocks, kOmpWarps * 32, smem, st>>>(jobs, njobs, total_chunks, chunk, queue,
+                                                       dev_err);
   return cudaGetLastError();
 }
 
@@ -347,11 +349,13 @@ cudaError_t launch_omp_batched_t(const OmpJob* jobs, int njobs, int64_t total_ch
 int omp_batch_chunk() { return kBatchChunk; }
 
 cudaError_t launch_omp_batched(const OmpJob* jobs_dev, int njobs, int64_t total_chunks, int tmax,
-                               unsigned long long* queue, int* dev_err, cudaStream_t st) {
+                               int chunk, unsigned long long* queue, int* dev_err,
+                               cudaStream_t st) {
   if (njobs <= 0 || total_chunks <= 0) return cudaSuccess;
-  if (tmax < 1 || tmax > kMaxT) return cudaErrorInvalidValue;
-  if (tmax <= 32) return launch_omp_batched_t<32>(jobs_dev, njobs, total_chunks, queue, dev_err, st);
-  return launch_omp_batched_t<64>(jobs_dev, njobs, total_chunks, queue, dev_err, st);
+  if (tmax < 1 || tmax > kMaxT || chunk < 1) return cudaErrorInvalidValue;
+  if (tmax <= 32)
+    return launch_omp_batched_t<32>(jobs_dev, njobs, total_chunks, chunk, queue, dev_err, st);
+  return launch_omp_batched_t<64>(jobs_dev, njobs, total_chunks, chunk, queue, dev_err, st);
 }
 
 int omp_padded_k(int K) {
@@ -360,12 +364,12 @@ int omp_padded_k(int K) {
 
 cudaError_t launch_omp(const float* G, int64_t ldg, const float* A0, int64_t lda, int K,
                        int64_t N, int T, const float* xnorm2, const float* eps2, int32_t* idx,
-                       float* coef, int32_t* nnz, int* dev_err, cudaStream_t st) {
+                       float* coef, int32_t* nnz, int* dev_err, cudaStream_t st, int grid_mult) {
   if (N <= 0) return cudaSuccess;
   if (K < 1 || K > kMaxK || T < 1 || T > kMaxT) return cudaErrorInvalidValue;
   const int kp = omp_padded_k(K);   // the lanes touch rows [0, kp) of every column
   if (ldg < kp || lda < kp || (ldg & 3) || (lda & 3)) return cudaErrorInvalidValue;
-#define KSVD_OMP_ARGS G, ldg, A0, lda, K, N, T, xnorm2, eps2, idx, coef, nnz, dev_err, st
+#define KSVD_OMP_ARGS G, ldg, A0, lda, K, N, T, xnorm2, eps2, idx, coef, nnz, dev_err, grid_mult, st
   if (T <= 32) {
     switch (kp) {
       case 128: return launch_omp_t<4, 32>(KSVD_OMP_ARGS);

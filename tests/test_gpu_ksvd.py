@@ -348,3 +348,33 @@ def test_iterate_graph_replay_matches_plain_launches(cuda, precision):
     np.testing.assert_allclose(rb, ra, rtol=1e-6)
     assert rel_rmse(Db.cpu().numpy(), Da.cpu().numpy()) <= 1e-5
     assert (ia == ib).float().mean().item() >= 0.999
+
+
+def test_autotune_keeps_inputs_and_results(cuda):
+    """ksvd_autotune picks launch shapes from its candidate sets, leaves D, X and the atom-order
+    stream untouched, and the tuned handle computes what an untuned one does."""
+    import torch
+
+    from ksvd_gb300 import Handle, datagen
+
+    p = datagen.make_problem("cfg0", N=6000, dict_from="extra")
+    c = p["cfg"]
+    X = torch.from_numpy(np.ascontiguousarray(np.asarray(p["X"], np.float32).T)).to(cuda)
+    D0 = torch.from_numpy(np.ascontiguousarray(np.asarray(p["D"], np.float32).T)).to(cuda)
+    X0c, D0c = X.clone(), D0.clone()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    h = Handle(c.n, c.K, c.T)
+    t = h.autotune(D0, X)
+    assert t["tuned"] == 1 and t["omp_grid_mult"] in (1, 2, 4, 8, 16)
+    assert t["sweep_ctas"] in (0, max(1, sms // 2), max(1, sms // 4))
+    assert torch.equal(X, X0c) and torch.equal(D0, D0c) and h.perm_draws == 0
+    Da = D0.clone()
+    ra = h.iterate(Da, X, 2)[3]
+    hb = Handle(c.n, c.K, c.T)
+    Db = D0.clone()
+    rb = hb.iterate(Db, X, 2)[3]
+    np.testing.assert_allclose(ra, rb, rtol=1e-4)
+    hb.tuning = t
+    assert hb.tuning == t
+    h.close()
+    hb.close()
