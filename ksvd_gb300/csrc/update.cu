@@ -519,15 +519,22 @@ struct Sweep {
 
   // New coefficients of atom j for this CTA's share of its signals, by warps [0, gnw).  Adds
   // into cpart (C row j) and *use_cnt; the caller synchronises and flushes.
-  __device__ void update_coefs(int j, int64_t q0, int64_t cnt, float anorm, int buf, int gw,
-                               int gnw, int* use_cnt) {
+  // Warps pull batches of EB entries from a shared counter (*next, zeroed before the phase), so
+  // the warps that finish their other work of the phase join in.
+  __device__ void update_coefs(int j, int64_t q0, int64_t cnt, float anorm, int buf, int* next,
+                               int* use_cnt) {
     const int n = A.n, K = A.K, T = A.T;
     const float aDj = aD_s[j];
     const int64_t per = (cnt + nctas - 1) / nctas;
     const int64_t qa = q0 + min(cnt, (int64_t)c * per), qb = q0 + min(cnt, (int64_t)(c + 1) * per);
     const int32_t* st = stage + buf * kStageCap;
     int my_use = 0;
-    for (int64_t qs = qa + (int64_t)gw * EB; qs < qb; qs += (int64_t)gnw * EB) {
+    for (;;) {
+      int bidx = 0;
+      if (lane == 0) bidx = atomicAdd(next, 1);
+      bidx = __shfl_sync(KSVD_FULL_MASK, bidx, 0);
+      const int64_t qs = qa + (int64_t)bidx * EB;
+      if (qs >= qb) break;
       const int ne = (int)min((int64_t)EB, qb - qs);
       int64_t e[EB], s[EB];
 #pragma unroll
@@ -695,6 +702,7 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
   __shared__ int red_i[64];
   __shared__ int sflag;
   __shared__ int use_cnt;
+  __shared__ int next_batch;
   Sweep<NPL> S(A, sm, red_f, red_i, &sflag);
   const int K = A.K, n = A.n, tid = threadIdx.x;
   constexpr int HALF = Sweep<NPL>::HALF;
@@ -726,7 +734,7 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
     float* av_next = A.avec + ((jj + 1) % 3) * n;
     float* av_clear = A.avec + ((jj + 2) % 3) * n;
     float* ad_next = A.aDbuf + ((jj + 1) & 1) * A.Kp;
-    if (tid == 0) use_cnt = 0;
+    if (tid == 0) { use_cnt = 0; next_batch = 0; }
     const float anorm = S.correct(j, prev, jn, A.avec + (jj % 3) * n, A.aDbuf + (jj & 1) * A.Kp);
     const int64_t q0 = A.start[j], cnt = A.start[j + 1] - q0;
     if (cnt == 0) {
@@ -740,9 +748,10 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
       }
     } else if (tid < HALF) {
       // warps 0..7: atom j's new coefficients
-      S.update_coefs(j, q0, cnt, anorm, jj & 1, tid >> 5, HALF >> 5, &use_cnt);
+      S.update_coefs(j, q0, cnt, anorm, jj & 1, &next_batch, &use_cnt);
     } else {
-      // warps 8..15: d_j, G/P rows of j, the next atom's partials, prefetch
+      // warps 8..15: d_j, G/P rows of j, the next atom's partials, prefetch; then they help
+      // with the coefficients
       const int gt = tid - HALF;
       if (S.c == 0)
         for (int r = gt; r < n; r += HALF) A.D[(int64_t)j * n + r] = S.a_s[r] / anorm;
@@ -752,6 +761,7 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
         S.zero_row(jn, gt, HALF);
         S.prefetch_next(jn, (jj + 1) & 1, gt, HALF);
       }
+      S.update_coefs(j, q0, cnt, anorm, jj & 1, &next_batch, &use_cnt);
     }
     __syncthreads();
     if (cnt > 0) S.flush_row(j, &use_cnt);
