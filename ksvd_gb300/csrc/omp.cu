@@ -53,15 +53,14 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G, int64_t 
   constexpr int LS = TMAX + 1;   // row stride of L in shared memory
   const int lane = threadIdx.x & 31;
   {
-    float2 al[M4][2];                  // alpha rows 128m + 4 lane + {0,1 | 2,3} as packed pairs
+    float al[M4][4];
     const float* a0p = a0col + 4 * lane;
     __syncwarp();                      // the previous signal's last reads of a0s are done
 #pragma unroll
     for (int m = 0; m < M4; ++m) {
       const float4 v = __ldcs(reinterpret_cast<const float4*>(a0p + 128 * m));
       *reinterpret_cast<float4*>(a0s + 128 * m + 4 * lane) = v;
-      al[m][0] = make_float2(v.x, v.y);
-      al[m][1] = make_float2(v.z, v.w);
+      al[m][0] = v.x; al[m][1] = v.y; al[m][2] = v.z; al[m][3] = v.w;
     }
     __syncwarp();
     int ind[SPL];
@@ -81,9 +80,8 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G, int64_t 
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           const int k = 128 * m + 4 * lane + q;
-          const float a = (q & 1) ? al[m][q >> 1].y : al[m][q >> 1].x;
-          const float v = a * a;
-          if (k < K && v > bv) { bv = v; bk = k; bal = a; }
+          const float v = al[m][q] * al[m][q];
+          if (k < K && v > bv) { bv = v; bk = k; bal = al[m][q]; }
         }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
@@ -171,27 +169,29 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G, int64_t 
 #pragma unroll
         for (int m = 0; m < M4; ++m)
 #pragma unroll
-          for (int q = 0; q < 2; ++q) al[m][q] = make_float2(0.f, 0.f);
+          for (int q = 0; q < 4; ++q) al[m][q] = 0.f;
 #pragma unroll 2
         for (int r = 0; r < i; ++r) {
           const int rl = r & 31, rj = r >> 5;
           const float cr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(c, rj), rl);
-          const float2 cr2 = make_float2(cr, cr);
           const int col = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(ind, rj), rl);
           const float* gp = G + (int64_t)col * ldg + 4 * lane;
 #pragma unroll
           for (int m = 0; m < M4; ++m) {
             const float4 g = __ldg(reinterpret_cast<const float4*>(gp + 128 * m));
-            // packed FP32 FMA (two lanes of alpha per instruction; same rounding as fmaf)
-            al[m][0] = __ffma2_rn(make_float2(g.x, g.y), cr2, al[m][0]);
-            al[m][1] = __ffma2_rn(make_float2(g.z, g.w), cr2, al[m][1]);
+            al[m][0] = fmaf(g.x, cr, al[m][0]);
+            al[m][1] = fmaf(g.y, cr, al[m][1]);
+            al[m][2] = fmaf(g.z, cr, al[m][2]);
+            al[m][3] = fmaf(g.w, cr, al[m][3]);
           }
         }
 #pragma unroll
         for (int m = 0; m < M4; ++m) {
           const float4 a = *reinterpret_cast<const float4*>(a0s + 128 * m + 4 * lane);
-          al[m][0] = make_float2(a.x - al[m][0].x, a.y - al[m][0].y);
-          al[m][1] = make_float2(a.z - al[m][1].x, a.w - al[m][1].y);
+          al[m][0] = a.x - al[m][0];
+          al[m][1] = a.y - al[m][1];
+          al[m][2] = a.z - al[m][2];
+          al[m][3] = a.w - al[m][3];
         }
       }
     }

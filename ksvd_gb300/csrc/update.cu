@@ -175,26 +175,19 @@ prepare_kernel(const float* __restrict__ X, int n, int T, int Kp, const int32_t*
 #pragma unroll
   for (int i = 0; i < NPL; ++i) acc[i] = 0.f;
   float g2 = 0.f;
-  auto scatter = [&](int64_t s, float g) {
-    const int nz = min(nnz[s], T);
-    for (int t = lane; t < nz; t += 32) {
-      const int i = idx[s * T + t];
-      if (i >= 0 && i < Kp) cw[i] = fmaf(g, coef[s * T + t], cw[i]);   // distinct per signal
-    }
-    __syncwarp();
-  };
   constexpr int EB = NPL <= 8 ? 4 : (NPL <= 16 ? 2 : 1);      // entries in flight per warp
   for (int64_t qs = q0 + (int64_t)w * EB; qs < q1; qs += (int64_t)NW * EB) {
     const int ne = (int)min((int64_t)EB, q1 - qs);
     int64_t sg[EB];
-    float gv[EB];
-    float xv[EB][NPL];
+    int ts[EB];
 #pragma unroll
     for (int b = 0; b < EB; ++b) {
       const int64_t e = b < ne ? list[qs + b] : 0;
       sg[b] = e / T;
-      gv[b] = b < ne ? coef[e] : 0.f;
+      ts[b] = (int)(e - sg[b] * T);
     }
+    // the signals, their whole code rows and support sizes: one round of independent loads
+    float xv[EB][NPL];
 #pragma unroll
     for (int b = 0; b < EB; ++b)
 #pragma unroll
@@ -202,15 +195,37 @@ prepare_kernel(const float* __restrict__ X, int n, int T, int Kp, const int32_t*
         const int r = lane + 32 * i;
         xv[b][i] = (b < ne && r < n) ? __ldg(X + sg[b] * n + r) : 0.f;
       }
+    float cf[EB][2];
+    int ix[EB][2], nz[EB];
 #pragma unroll
     for (int b = 0; b < EB; ++b) {
+      nz[b] = b < ne ? nnz[sg[b]] : 0;
 #pragma unroll
-      for (int i = 0; i < NPL; ++i) acc[i] = fmaf(gv[b], xv[b][i], acc[i]);
-      g2 = fmaf(gv[b], gv[b], g2);
+      for (int u = 0; u < 2; ++u) {
+        const int t = lane + 32 * u;
+        const bool in = b < ne && t < T;
+        ix[b][u] = in ? idx[sg[b] * T + t] : -1;
+        cf[b][u] = in ? coef[sg[b] * T + t] : 0.f;
+      }
     }
 #pragma unroll
-    for (int b = 0; b < EB; ++b)
-      if (b < ne) scatter(sg[b], gv[b]);
+    for (int b = 0; b < EB; ++b) {
+      // gamma_j(s) is slot ts of the code row
+      const float g = __shfl_sync(KSVD_FULL_MASK, (ts[b] >> 5) == 0 ? cf[b][0] : cf[b][1],
+                                  ts[b] & 31);
+      if (b >= ne) continue;
+#pragma unroll
+      for (int i = 0; i < NPL; ++i) acc[i] = fmaf(g, xv[b][i], acc[i]);
+      g2 = fmaf(g, g, g2);
+      const int lim = min(nz[b], T);
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int t = lane + 32 * u;
+        const int i = ix[b][u];
+        if (t < lim && i >= 0 && i < Kp) cw[i] = fmaf(g, cf[b][u], cw[i]);   // distinct per signal
+      }
+      __syncwarp();
+    }
   }
 #pragma unroll
   for (int i = 0; i < NPL; ++i) {
@@ -274,23 +289,22 @@ __device__ __forceinline__ void prefetch_l2_bulk(const void* p, uint32_t bytes) 
 
 // Generation barrier over all CTAs of the cooperative launch.  Bounded: returns false (and
 // records kDevErrTimeout) if the generation does not advance within the spin limit.
-__device__ bool grid_barrier(unsigned* bar, unsigned nctas, int* dev_err, int* sflag) {
+// Grid barrier on a monotonic arrival counter (zeroed by init_state_kernel before the launch):
+// barrier number e of the launch is passed once e * nctas CTAs have arrived.  Arriving is one
+// fire-and-forget atomic add, so the last CTA to arrive releases the others without a second
+// round trip; a spin that runs past kBarrierSpinLimit polls records a timeout and gives up.
+__device__ bool grid_barrier(unsigned* bar, unsigned nctas, unsigned* epoch, int* dev_err,
+                             int* sflag) {
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    const unsigned gen = ld_acquire_gpu(bar + 1);
+    const unsigned target = (++*epoch) * nctas;
     __threadfence();
-    const unsigned arrived = atomicAdd(bar, 1u) + 1u;
-    if (arrived == nctas) {
-      atomicExch(bar, 0u);
-      __threadfence();
-      atomicAdd(bar + 1, 1u);
-    } else {
-      unsigned spins = 0;
-      while (ld_acquire_gpu(bar + 1) == gen) {
-        if (++spins > kBarrierSpinLimit) { ok = 0; atomicOr(dev_err, kDevErrTimeout); break; }
-        if (spins > 4096) __nanosleep(100);
-      }
+    atomicAdd(bar, 1u);
+    unsigned spins = 0;
+    while (ld_acquire_gpu(bar) < target) {
+      if (++spins > kBarrierSpinLimit) { ok = 0; atomicOr(dev_err, kDevErrTimeout); break; }
+      if (spins > 4096) __nanosleep(100);
     }
     *sflag = ok;
   }
@@ -363,7 +377,8 @@ struct Sweep {
     k1 = min(A.K, k0 + kper);
   }
 
-  __device__ bool barrier() { return grid_barrier(A.barrier, nctas, A.dev_err, sflag); }
+  unsigned epoch = 0;   // barriers passed (thread 0's copy is the one used)
+  __device__ bool barrier() { return grid_barrier(A.barrier, nctas, &epoch, A.dev_err, sflag); }
 
   __device__ float v_entry(int k, int jn, int jx) const {
     return (k >= A.K || k == jx) ? 0.f

@@ -378,3 +378,35 @@ def test_autotune_keeps_inputs_and_results(cuda):
     assert hb.tuning == t
     h.close()
     hb.close()
+
+
+def test_reference_recorded_dictionary_thirty_iterations(oracle_mod, cuda):
+    """The reference's own run shape (n=300, K=9, N=3600, T=6, 30 iterations, ProgramParameters
+    and Matlab/fmriKSVD.m) started from its recorded initial dictionary (input/D.mat, frozen as
+    tests/golden/ref_D_300x9.npy): every iteration's RMSE against the FP64 oracle, and the dense
+    code has exactly T = 6 nonzeros per signal like the recorded CUDA_Gamma outputs."""
+    import os
+
+    from ksvd_gb300 import Handle, random_permutation
+
+    Dref = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_D_300x9.npy"))
+    rng = np.random.default_rng(300)
+    n, K, N, T = 300, 9, 3600, 6
+    Dn = Dref / np.linalg.norm(Dref, axis=0)
+    X = np.zeros((n, N))
+    for s in range(N):
+        S = rng.choice(K, T, replace=False)
+        X[:, s] = Dn[:, S] @ rng.standard_normal(T)
+    X += 0.1 * rng.standard_normal((n, N)) * np.linalg.norm(X, axis=0) / np.sqrt(n)
+    D0 = Dref + 0.3 * rng.standard_normal(Dref.shape) * np.linalg.norm(Dref, axis=0) / np.sqrt(n)
+    X, D0 = X.astype(np.float32), D0.astype(np.float32)
+    perms = np.stack([random_permutation(11, it, K) for it in range(30)])
+    _, ri, rc, rn, rr = oracle_mod.ksvd(X.astype(np.float64), D0.astype(np.float64), T, 30, perms)
+    h = Handle(n, K, T)
+    Dd = to_dev(D0, cuda)
+    idx, coef, nnz, rmse = h.iterate(Dd, to_dev(X, cuda), 30, perms)
+    np.testing.assert_allclose(rmse, rr, rtol=1e-3)
+    G = h.dense_gamma(idx, coef, nnz).cpu().numpy()        # (N, K): CUDA_Gamma transposed
+    assert G.shape == (N, K)
+    assert np.all((G != 0).sum(axis=1) == T)
+    h.close()
