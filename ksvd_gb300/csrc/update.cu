@@ -283,8 +283,13 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
   return v;
 }
 
-__device__ __forceinline__ void prefetch_l2_bulk(const void* p, uint32_t bytes) {
-  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+// L2 prefetch of every 128-byte line of [p, p + bytes), one fire-and-forget instruction per line
+// through the load/store path (bulk prefetches would queue on the SM's single TMA unit).
+__device__ __forceinline__ void prefetch_l2_lines(const void* p, uint32_t bytes) {
+  const uintptr_t a0 = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(127);
+  const uintptr_t a1 = reinterpret_cast<uintptr_t>(p) + bytes;
+  for (uintptr_t a = a0; a < a1; a += 128)
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(a) : "memory");
 }
 
 // Generation barrier over all CTAs of the cooperative launch.  Bounded: returns false (and
@@ -355,6 +360,7 @@ struct Sweep {
   float* cpart;    // Kp    this CTA's part of the new row j of C
   float* v_s;      // Kp    C(:, j') for the next atom (its left-out entry 0)
   int32_t* stage;  // 2 x kStageCap: this CTA's list entries of the current / next atom
+  int32_t* pos;    // Kp: position of every atom in this sweep's order
   float* red_f;
   int* red_i;
   int* sflag;
@@ -367,6 +373,7 @@ struct Sweep {
     cpart = aD_s + A.Kp;
     v_s = cpart + A.Kp;
     stage = reinterpret_cast<int32_t*>(v_s + A.Kp);
+    pos = stage + 2 * kStageCap;
     tid = threadIdx.x;
     lane = tid & 31;
     w = tid >> 5;
@@ -517,18 +524,14 @@ struct Sweep {
     if (cnt == 0) return;
     const int64_t per = (cnt + nctas - 1) / nctas;
     const int64_t qa = q0 + min(cnt, (int64_t)c * per), qb = q0 + min(cnt, (int64_t)(c + 1) * per);
-    const bool bulk_x = (A.n & 3) == 0, bulk_c = (A.T & 3) == 0;
     int32_t* st = stage + buf * kStageCap;
     for (int64_t q = qa + gt; q < qb; q += gsize) {
       const int32_t e = A.list[q];
       if (q - qa < kStageCap) st[q - qa] = e;
       const int64_t s = e / A.T;
-      const float* x = A.X + s * A.n;
-      if (bulk_x) prefetch_l2_bulk(x, (uint32_t)A.n * 4);
-      if (bulk_c) {
-        prefetch_l2_bulk(A.coef + s * A.T, (uint32_t)A.T * 4);
-        prefetch_l2_bulk(A.idx + s * A.T, (uint32_t)A.T * 4);
-      }
+      prefetch_l2_lines(A.X + s * A.n, (uint32_t)A.n * 4);
+      prefetch_l2_lines(A.coef + s * A.T, (uint32_t)A.T * 4);
+      prefetch_l2_lines(A.idx + s * A.T, (uint32_t)A.T * 4);
     }
   }
 
@@ -636,10 +639,12 @@ struct Sweep {
   }
 
   // After a CTA barrier: this CTA's part of C row j and of atom j's use count.
-  __device__ void flush_row(int j, const int* use_cnt) {
+  // C(k, j) is read again only when atom k comes later in this sweep (its v = C(k, :)), so
+  // the atoms already processed are skipped.
+  __device__ void flush_row(int j, int jj, const int* use_cnt) {
     for (int k = tid; k < A.K; k += blockDim.x) {
       const float v = cpart[k];
-      if (k != j && v != 0.f) atomicAdd(A.C + (int64_t)k * A.Kp + j, v);
+      if (k != j && v != 0.f && pos[k] > jj) atomicAdd(A.C + (int64_t)k * A.Kp + j, v);
     }
     if (tid == 0 && *use_cnt) atomicAdd(A.usecount + j, *use_cnt);
   }
@@ -724,9 +729,12 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
   const int32_t* perm = A.perm + (A.iter_ctr ? (int64_t)(*A.iter_ctr) * K : 0);
   // every CTA checks the whole permutation itself, so all of them leave together or none does
   int bad = 0;
+  for (int k = tid; k < A.Kp; k += blockDim.x) S.pos[k] = K;   // (an order with repeats: no skips)
+  __syncthreads();
   for (int k = tid; k < K; k += blockDim.x) {
     const int j = perm[k];
     bad |= (j < 0 || j >= K);
+    if (j >= 0 && j < K) S.pos[j] = k;
   }
   if (__syncthreads_or(bad)) {
     if (blockIdx.x == 0 && tid == 0) atomicOr(A.dev_err, kDevErrBounds);
@@ -779,7 +787,7 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
       S.update_coefs(j, q0, cnt, anorm, jj & 1, &next_batch, &use_cnt);
     }
     __syncthreads();
-    if (cnt > 0) S.flush_row(j, &use_cnt);
+    if (cnt > 0) S.flush_row(j, jj, &use_cnt);
     if (S.c == 0)
       for (int r = tid; r < n; r += blockDim.x) av_clear[r] = 0.f;
     if (!S.barrier()) return;
@@ -845,7 +853,7 @@ cudaError_t launch_update_sweep(const UpdateArgs& a, cudaStream_t st) {
   s.replaced = a.replaced; s.counter = a.counter; s.usecount = a.usecount; s.barrier = a.barrier;
   s.dev_err = a.dev_err;
   const size_t smem = sizeof(float) * ((size_t)a.n + 3 * (size_t)a.Kp) +
-                      sizeof(int32_t) * 2 * kStageCap;
+                      sizeof(int32_t) * (2 * kStageCap + (size_t)a.Kp);
   const int npl = (a.n + 31) / 32;
   auto launch = [&](auto kern) -> cudaError_t {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
