@@ -416,7 +416,10 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp32", "mixed"],
+                    help="mixed (default): BF16 tensor-core GEMMs; the plain FP32 path is also "
+                         "timed on the same workload for the ratio unless --no-compare")
+    ap.add_argument("--no-compare", action="store_true")
     ap.add_argument("--config", default="cfg2")
     ap.add_argument("--cpu-sample", type=int, default=50000)
     ap.add_argument("--signals", type=int, default=None,
@@ -466,6 +469,7 @@ def main():
                                 seed=datagen.SEED_BASE + cfg.index + 1000 * rank, device="cuda")
     X, D = prob["X"], prob["D"]
     N = X.shape[0]
+    D0 = D.clone()
     # timed handle: iterations 2..K of each call replay a CUDA graph of one iteration;
     # a second, profiling handle measures per-stage times (events) in a separate pass
     h = Handle(cfg.n, cfg.K, cfg.T, precision=args.precision, graph=not args.no_graph)
@@ -496,6 +500,33 @@ def main():
         ms = float(t.item())
     value = ws * args.steps / (ms / 1e3)
     replays = h.graph_replays()
+    # the plain FP32 path on the same workload from the same initial dictionary (the ratio the
+    # mixed path is measured against; RMSE compared iteration by iteration)
+    fp32_leg = None
+    if args.precision == "mixed" and not args.no_compare:
+        hf = Handle(cfg.n, cfg.K, cfg.T, precision="fp32", graph=not args.no_graph)
+        hf.tuning = hf.autotune(D0, X)
+        Df = D0.clone()
+        rf = list(hf.iterate(Df, X, args.warmup, out=out)[3])
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        rf += list(hf.iterate(Df, X, args.steps, out=out)[3])
+        f1.record(stream)
+        torch.cuda.synchronize()
+        fms = f0.elapsed_time(f1)
+        if dist:
+            t = torch.tensor([fms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            fms = float(t.item())
+        fval = ws * args.steps / (fms / 1e3)
+        fp32_leg = {"value": fval, "unit": "iter/s", "ms_per_step": fms / args.steps,
+                    "mixed_over_fp32": value / fval,
+                    "rmse_last_fp32": rf[-1], "rmse_last_mixed": rms[-1],
+                    "rmse_max_rel_diff": max(abs(a - b) / b for a, b in zip(rms, rf))}
+        hf.close()
     hp.iterate(D, X, 1, out=out)                  # warm the profiling handle's workspace
     hp.stage_times(reset=True)
     hp.iterate(D, X, min(args.steps, 5), out=out)
@@ -579,6 +610,7 @@ def main():
                                   "unit": "signals/s", "stages": "D'X + Batch-OMP"},
             "stages": stage_summary,
             "roofline": roof,
+            "fp32_path": fp32_leg,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": KERNELS_PER_CALL[args.precision] +

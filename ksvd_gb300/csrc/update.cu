@@ -176,15 +176,28 @@ prepare_kernel(const float* __restrict__ X, int n, int T, int Kp, const int32_t*
   for (int i = 0; i < NPL; ++i) acc[i] = 0.f;
   float g2 = 0.f;
   constexpr int EB = NPL <= 8 ? 4 : (NPL <= 16 ? 2 : 1);      // entries in flight per warp
+  // the list entries of the warp's next batch are loaded one batch ahead, so each batch costs
+  // one round of loads (signals and code rows) instead of two
+  int32_t ecur[EB];
+#pragma unroll
+  for (int b = 0; b < EB; ++b) {
+    const int64_t q = q0 + (int64_t)w * EB + b;
+    ecur[b] = q < q1 ? list[q] : 0;
+  }
   for (int64_t qs = q0 + (int64_t)w * EB; qs < q1; qs += (int64_t)NW * EB) {
     const int ne = (int)min((int64_t)EB, q1 - qs);
     int64_t sg[EB];
     int ts[EB];
 #pragma unroll
     for (int b = 0; b < EB; ++b) {
-      const int64_t e = b < ne ? list[qs + b] : 0;
+      const int64_t e = b < ne ? ecur[b] : 0;
       sg[b] = e / T;
       ts[b] = (int)(e - sg[b] * T);
+    }
+#pragma unroll
+    for (int b = 0; b < EB; ++b) {
+      const int64_t q = qs + (int64_t)NW * EB + b;
+      ecur[b] = q < q1 ? list[q] : 0;
     }
     // the signals, their whole code rows and support sizes: one round of independent loads
     float xv[EB][NPL];
