@@ -420,6 +420,8 @@ def main():
                     help="mixed (default): BF16 tensor-core GEMMs; the plain FP32 path is also "
                          "timed on the same workload for the ratio unless --no-compare")
     ap.add_argument("--no-compare", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="built-in launch shapes (profiler captures count launches from the start)")
     ap.add_argument("--config", default="cfg2")
     ap.add_argument("--cpu-sample", type=int, default=50000)
     ap.add_argument("--signals", type=int, default=None,
@@ -474,8 +476,9 @@ def main():
     # a second, profiling handle measures per-stage times (events) in a separate pass
     h = Handle(cfg.n, cfg.K, cfg.T, precision=args.precision, graph=not args.no_graph)
     hp = Handle(cfg.n, cfg.K, cfg.T, precision=args.precision, profile=True)
-    tuning = h.autotune(D, X)                     # launch shapes timed on this workload
-    hp.tuning = tuning
+    tuning = None if args.no_autotune else h.autotune(D, X)   # launch shapes timed on this workload
+    if tuning:
+        hp.tuning = tuning
     idx, coef, nnz = h._code(N, dev)
     out = (idx, coef, nnz)
     rms = list(h.iterate(D, X, args.warmup, out=out)[3])
@@ -505,7 +508,8 @@ def main():
     fp32_leg = None
     if args.precision == "mixed" and not args.no_compare:
         hf = Handle(cfg.n, cfg.K, cfg.T, precision="fp32", graph=not args.no_graph)
-        hf.tuning = hf.autotune(D0, X)
+        if not args.no_autotune:
+            hf.tuning = hf.autotune(D0, X)
         Df = D0.clone()
         rf = list(hf.iterate(Df, X, args.warmup, out=out)[3])
         if dist:
@@ -525,7 +529,8 @@ def main():
         fp32_leg = {"value": fval, "unit": "iter/s", "ms_per_step": fms / args.steps,
                     "mixed_over_fp32": value / fval,
                     "rmse_last_fp32": rf[-1], "rmse_last_mixed": rms[-1],
-                    "rmse_max_rel_diff": max(abs(a - b) / b for a, b in zip(rms, rf))}
+                    "rmse_max_rel_diff": max(abs(a - b) / b for a, b in zip(rms, rf)),
+                    "rmse_per_iter_mixed": rms, "rmse_per_iter_fp32": rf}
         hf.close()
     hp.iterate(D, X, 1, out=out)                  # warm the profiling handle's workspace
     hp.stage_times(reset=True)

@@ -57,11 +57,13 @@ __device__ __forceinline__ void gemm_tile(const float* __restrict__ A, int64_t l
     }
   };
 
-  float acc[8][8];
+  // accumulators as packed pairs (acc2[i][jp] = outputs (i, 2jp) and (i, 2jp+1)): one packed
+  // FP32 FMA per two outputs halves the issue slots of the inner product (same rounding as fmaf)
+  float2 acc2[8][4];
 #pragma unroll
   for (int i = 0; i < 8; ++i)
 #pragma unroll
-    for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+    for (int j = 0; j < 4; ++j) acc2[i][j] = make_float2(0.0f, 0.0f);
 
   const int nk = (inner + BK - 1) / BK;
   load(0);
@@ -77,11 +79,14 @@ __device__ __forceinline__ void gemm_tile(const float* __restrict__ A, int64_t l
       float4 b0 = *reinterpret_cast<const float4*>(&Bs[buf][r][tx * 4]);
       float4 b1 = *reinterpret_cast<const float4*>(&Bs[buf][r][64 + tx * 4]);
       const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-      const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+      const float2 b2[4] = {make_float2(b0.x, b0.y), make_float2(b0.z, b0.w),
+                            make_float2(b1.x, b1.y), make_float2(b1.z, b1.w)};
 #pragma unroll
-      for (int i = 0; i < 8; ++i)
+      for (int i = 0; i < 8; ++i) {
+        const float2 ai = make_float2(a[i], a[i]);
 #pragma unroll
-        for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+        for (int j = 0; j < 4; ++j) acc2[i][j] = __ffma2_rn(ai, b2[j], acc2[i][j]);
+      }
     }
     if (kt + 1 < nk) {
       store(buf ^ 1);
@@ -89,6 +94,14 @@ __device__ __forceinline__ void gemm_tile(const float* __restrict__ A, int64_t l
     }
   }
 
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      acc[i][2 * j] = acc2[i][j].x;
+      acc[i][2 * j + 1] = acc2[i][j].y;
+    }
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
     const int64_t s = n0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + (j - 4));
