@@ -138,6 +138,23 @@ MEASURED_TRAFFIC = {("omp", 256, 1024, 16): (414.642432e6 + 7.440128e6) / 100_00
 FP32_SIMT_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 
 
+def max_over_ranks(x, dist, device):
+    """The slowest rank's time (every rank gets it); identity without a process group."""
+    if dist is None:
+        return float(x)
+    import torch
+
+    t = torch.tensor([float(x)], device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rate(units_per_rank, steps, ms, world):
+    """Whole-job throughput: every rank processes `units_per_rank` per step (weak scaling),
+    timed by the slowest rank."""
+    return world * units_per_rank * steps / (ms / 1e3)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -496,12 +513,8 @@ def main():
     torch.cuda.synchronize()
     t_wall = time.perf_counter() - t_wall
     clocks = sampler.stop()
-    ms = e0.elapsed_time(e1)
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * args.steps / (ms / 1e3)
+    ms = max_over_ranks(e0.elapsed_time(e1), dist, dev)
+    value = aggregate_rate(1, args.steps, ms, ws)
     replays = h.graph_replays()
     # the plain FP32 path on the same workload from the same initial dictionary (the ratio the
     # mixed path is measured against; RMSE compared iteration by iteration)
@@ -520,12 +533,8 @@ def main():
         rf += list(hf.iterate(Df, X, args.steps, out=out)[3])
         f1.record(stream)
         torch.cuda.synchronize()
-        fms = f0.elapsed_time(f1)
-        if dist:
-            t = torch.tensor([fms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            fms = float(t.item())
-        fval = ws * args.steps / (fms / 1e3)
+        fms = max_over_ranks(f0.elapsed_time(f1), dist, dev)
+        fval = aggregate_rate(1, args.steps, fms, ws)
         fp32_leg = {"value": fval, "unit": "iter/s", "ms_per_step": fms / args.steps,
                     "mixed_over_fp32": value / fval,
                     "rmse_last_fp32": rf[-1], "rmse_last_mixed": rms[-1],
@@ -587,12 +596,8 @@ def main():
         for _ in range(e2e_steps):
             h.iterate_host(Dn, Xn, 1, out=(oi, oc, on))
         torch.cuda.synchronize()
-        te = time.perf_counter() - t0
-        if dist:
-            t = torch.tensor([te], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            te = float(t.item())
-        e2e = {"value": ws * e2e_steps / te, "unit": "iter/s",
+        te = max_over_ranks(time.perf_counter() - t0, dist, dev)
+        e2e = {"value": aggregate_rate(1, e2e_steps, te * 1e3, ws), "unit": "iter/s",
                "h2d_bytes_per_step": int(X.numel() * 4 + D.numel() * 4),
                "d2h_bytes_per_step": int(D.numel() * 4 + N * cfg.T * 8 + N * 4 + 8),
                "steps": e2e_steps}
