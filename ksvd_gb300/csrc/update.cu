@@ -311,14 +311,21 @@ __device__ __forceinline__ void prefetch_l2_lines(const void* p, uint32_t bytes)
 // barrier number e of the launch is passed once e * nctas CTAs have arrived.  Arriving is one
 // fire-and-forget atomic add, so the last CTA to arrive releases the others without a second
 // round trip; a spin that runs past kBarrierSpinLimit polls records a timeout and gives up.
-__device__ bool grid_barrier(unsigned* bar, unsigned nctas, unsigned* epoch, int* dev_err,
-                             int* sflag) {
+// `deferred` runs on every thread after this CTA has arrived and before it waits: work whose
+// results no CTA reads before the following barrier overlaps the wait.
+template <typename F>
+__device__ bool grid_barrier_with(unsigned* bar, unsigned nctas, unsigned* epoch, int* dev_err,
+                                  int* sflag, F deferred) {
   __syncthreads();
+  const unsigned target = (*epoch + 1) * nctas;
   if (threadIdx.x == 0) {
-    int ok = 1;
-    const unsigned target = (++*epoch) * nctas;
+    ++*epoch;
     __threadfence();
     atomicAdd(bar, 1u);
+  }
+  deferred();
+  if (threadIdx.x == 0) {
+    int ok = 1;
     unsigned spins = 0;
     while (ld_acquire_gpu(bar) < target) {
       if (++spins > kBarrierSpinLimit) { ok = 0; atomicOr(dev_err, kDevErrTimeout); break; }
@@ -330,6 +337,11 @@ __device__ bool grid_barrier(unsigned* bar, unsigned nctas, unsigned* epoch, int
   const bool ok = *sflag != 0;
   __syncthreads();
   return ok;
+}
+
+__device__ bool grid_barrier(unsigned* bar, unsigned nctas, unsigned* epoch, int* dev_err,
+                             int* sflag) {
+  return grid_barrier_with(bar, nctas, epoch, dev_err, sflag, [] {});
 }
 
 struct SweepArgs {
@@ -399,6 +411,10 @@ struct Sweep {
 
   unsigned epoch = 0;   // barriers passed (thread 0's copy is the one used)
   __device__ bool barrier() { return grid_barrier(A.barrier, nctas, &epoch, A.dev_err, sflag); }
+  template <typename F>
+  __device__ bool barrier_with(F deferred) {
+    return grid_barrier_with(A.barrier, nctas, &epoch, A.dev_err, sflag, deferred);
+  }
 
   __device__ float v_entry(int k, int jn, int jx) const {
     return (k >= A.K || k == jx) ? 0.f
@@ -654,12 +670,16 @@ struct Sweep {
   // After a CTA barrier: this CTA's part of C row j and of atom j's use count.
   // C(k, j) is read again only when atom k comes later in this sweep (its v = C(k, :)), so
   // the atoms already processed are skipped.
-  __device__ void flush_row(int j, int jj, const int* use_cnt) {
+  // urgent: only the next two atoms' entries are read in the next phase (cp = C(j', j) and
+  // v = C(j'', :)); the rest is flushed while the CTA waits at the grid barrier.
+  __device__ void flush_row(int j, int jj, int k1n, int k2n, bool urgent, const int* use_cnt) {
     for (int k = tid; k < A.K; k += blockDim.x) {
+      const bool next_two = k == k1n || k == k2n;
+      if (next_two != urgent) continue;
       const float v = cpart[k];
       if (k != j && v != 0.f && pos[k] > jj) atomicAdd(A.C + (int64_t)k * A.Kp + j, v);
     }
-    if (tid == 0 && *use_cnt) atomicAdd(A.usecount + j, *use_cnt);
+    if (!urgent && tid == 0 && *use_cnt) atomicAdd(A.usecount + j, *use_cnt);
   }
 
   // The worst-represented of the first min(max_signals, N - counter) unused signals replaces
@@ -800,10 +820,14 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
       S.update_coefs(j, q0, cnt, anorm, jj & 1, &next_batch, &use_cnt);
     }
     __syncthreads();
-    if (cnt > 0) S.flush_row(j, jj, &use_cnt);
+    const int jn2 = jj + 2 < K ? perm[jj + 2] : -1;
+    if (cnt > 0) S.flush_row(j, jj, jn, jn2, true, &use_cnt);
     if (S.c == 0)
       for (int r = tid; r < n; r += blockDim.x) av_clear[r] = 0.f;
-    if (!S.barrier()) return;
+    if (!S.barrier_with([&] {
+          if (cnt > 0) S.flush_row(j, jj, jn, jn2, false, &use_cnt);
+        }))
+      return;
   }
 }
 
