@@ -573,6 +573,18 @@ def main():
     roof["peak_source"] = pk["src"]
     stage_summary = {k: {"ms_per_launch": round(v[0], 4), "share": round(v[0] * v[1] / sum(
         a * b for a, b in per.values()), 4)} for k, v in per.items()}
+    for k, v in stage_summary.items():
+        # each stage against its own roof: algorithmic HBM bytes (or tensor FLOPs) per launch
+        b = stage_bytes(cfg, N, k)
+        if b and not (k in ("dtx", "gram") and args.precision == "mixed"):
+            gbs = b / (v["ms_per_launch"] / 1e3) / 1e9
+            v["hbm_gbs"] = round(gbs, 1)
+            v["hbm_frac"] = round(gbs / pk["hbm"], 4)
+        elif k in ("dtx", "gram"):
+            tf = stage_flops(cfg, N, k) / (v["ms_per_launch"] / 1e3) / 1e12
+            v["tflops"] = round(tf, 1)
+            if args.precision == "mixed":
+                v["tensor_frac_3pass"] = round(3 * tf / pk["bf16"], 4)
     omp_ms = per.get("omp", (0, 0))[0] + per.get("dtx", (0, 0))[0]
 
     # end to end through the C ABI with pinned host buffers

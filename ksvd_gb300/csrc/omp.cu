@@ -22,6 +22,19 @@ namespace {
 
 constexpr int kOmpWarps = 8;
 
+// Shared-memory layout of the Cholesky factor L (TMAX x TMAX, lower): rows of stride TMAX+1
+// (bank-conflict padding) up to TMAX = 32; for TMAX = 64 packed by rows (row r at r(r+1)/2),
+// half the space, so two CTAs fit on an SM.
+template <int TMAX>
+__host__ __device__ constexpr int l_floats() {
+  return TMAX > 32 ? TMAX * (TMAX + 1) / 2 : TMAX * (TMAX + 1);
+}
+template <int TMAX>
+__device__ __forceinline__ int lidx(int r, int q) {
+  if constexpr (TMAX > 32) return r * (r + 1) / 2 + q;
+  else return r * (TMAX + 1) + q;
+}
+
 template <int SPL>
 __device__ __forceinline__ float pick(const float (&a)[SPL], int j) {
   if constexpr (SPL == 1) return a[0];
@@ -50,7 +63,6 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G, int64_t 
                                            bool& numeric_bad) {
   constexpr int M4 = KPL / 4;    // float4 groups per lane; lane owns rows 128*m + 4*lane + q
   constexpr int SPL = TMAX / 32; // support slots per lane; lane owns slots lane + 32*j
-  constexpr int LS = TMAX + 1;   // row stride of L in shared memory
   const int lane = threadIdx.x & 31;
   {
     float al[M4][4];
@@ -111,12 +123,12 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G, int64_t 
         }
         for (int r = 0; r < i; ++r) {
           const int rl = r & 31, rj = r >> 5;
-          const float wr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(b, rj), rl) / L[r * LS + r];
+          const float wr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(b, rj), rl) / L[lidx<TMAX>(r, r)];
           if (lane == rl) put<SPL>(w, rj, wr);
 #pragma unroll
           for (int j = 0; j < SPL; ++j) {
             const int q = lane + 32 * j;
-            if (q > r && q < i) b[j] = fmaf(-L[q * LS + r], wr, b[j]);
+            if (q > r && q < i) b[j] = fmaf(-L[lidx<TMAX>(q, r)], wr, b[j]);
           }
         }
         float ss = 0.f, wy = 0.f;
@@ -133,10 +145,10 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G, int64_t 
 #pragma unroll
         for (int j = 0; j < SPL; ++j) {
           const int q = lane + 32 * j;
-          if (q < i) L[i * LS + q] = w[j];
+          if (q < i) L[lidx<TMAX>(i, q)] = w[j];
         }
       }
-      if (lane == 0) L[i * LS + i] = Lii;
+      if (lane == 0) L[lidx<TMAX>(i, i)] = Lii;
       if (lane == (i & 31)) { put<SPL>(ind, i >> 5, p); put<SPL>(y, i >> 5, ynew); }
       ++i;
       __syncwarp();
@@ -155,12 +167,12 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G, int64_t 
         for (int j = 0; j < SPL; ++j) t[j] = y[j];
         for (int r = i - 1; r >= 0; --r) {
           const int rl = r & 31, rj = r >> 5;
-          const float cr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(t, rj), rl) / L[r * LS + r];
+          const float cr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(t, rj), rl) / L[lidx<TMAX>(r, r)];
           if (lane == rl) put<SPL>(c, rj, cr);
 #pragma unroll
           for (int j = 0; j < SPL; ++j) {
             const int q = lane + 32 * j;
-            if (q < r) t[j] = fmaf(-L[r * LS + q], cr, t[j]);
+            if (q < r) t[j] = fmaf(-L[lidx<TMAX>(r, q)], cr, t[j]);
           }
         }
       }
@@ -211,17 +223,16 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G, int64_t 
 }
 
 template <int KPL, int TMAX>
-__global__ void __launch_bounds__(kOmpWarps * 32, (TMAX <= 32 ? 3 : 1))
+__global__ void __launch_bounds__(kOmpWarps * 32, (TMAX <= 32 ? 3 : 2))
 omp_kernel(const float* __restrict__ G, int64_t ldg, const float* __restrict__ A0, int64_t lda,
            int K, int64_t N, int T, const float* __restrict__ xnorm2,
            const float* __restrict__ eps2, int32_t* __restrict__ idx_out,
            float* __restrict__ coef_out, int32_t* __restrict__ nnz_out, int* __restrict__ dev_err) {
-  constexpr int LS = TMAX + 1;
   extern __shared__ __align__(16) float smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  float* L = smem + (size_t)wib * (TMAX * LS + 32 * KPL);   // Cholesky factor, (TMAX x LS)
-  float* a0s = L + TMAX * LS;                                // this warp's alpha0 column
+  float* L = smem + (size_t)wib * (l_floats<TMAX>() + 32 * KPL);   // Cholesky factor
+  float* a0s = L + l_floats<TMAX>();                                // this warp's alpha0 column
   const int64_t warps_total = (int64_t)gridDim.x * kOmpWarps;
   bool numeric_bad = false;
   const bool emode = eps2 != nullptr;
@@ -240,15 +251,14 @@ omp_kernel(const float* __restrict__ G, int64_t ldg, const float* __restrict__ A
 constexpr int kBatchChunk = 16;   // default signals per work-queue chunk
 
 template <int TMAX>
-__global__ void __launch_bounds__(kOmpWarps * 32, (TMAX <= 32 ? 2 : 1))
+__global__ void __launch_bounds__(kOmpWarps * 32, 2)
 omp_batched_kernel(const OmpJob* __restrict__ jobs, int njobs, int64_t total_chunks,
                    int chunk, unsigned long long* __restrict__ queue, int* __restrict__ dev_err) {
-  constexpr int LS = TMAX + 1;
   extern __shared__ __align__(16) float smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  float* L = smem + (size_t)wib * (TMAX * LS + 32 * 32);
-  float* a0s = L + TMAX * LS;
+  float* L = smem + (size_t)wib * (l_floats<TMAX>() + 32 * 32);
+  float* a0s = L + l_floats<TMAX>();
   bool numeric_bad = false;
   for (;;) {
     unsigned long long c = 0;
@@ -303,7 +313,7 @@ cudaError_t launch_omp_t(const float* G, int64_t ldg, const float* A0, int64_t l
                          int64_t N, int T, const float* xnorm2, const float* eps2, int32_t* idx,
                          float* coef, int32_t* nnz, int* dev_err, int grid_mult,
                          cudaStream_t st) {
-  const size_t smem = (size_t)kOmpWarps * (TMAX * (TMAX + 1) + 32 * KPL) * sizeof(float);
+  const size_t smem = (size_t)kOmpWarps * (l_floats<TMAX>() + 32 * KPL) * sizeof(float);
   auto kern = omp_kernel<KPL, TMAX>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
@@ -324,7 +334,7 @@ cudaError_t launch_omp_t(const float* G, int64_t ldg, const float* A0, int64_t l
 template <int TMAX>
 cudaError_t launch_omp_batched_t(const OmpJob* jobs, int njobs, int64_t total_chunks, int chunk,
                                  unsigned long long* queue, int* dev_err, cudaStream_t st) {
-  const size_t smem = (size_t)kOmpWarps * (TMAX * (TMAX + 1) + 32 * 32) * sizeof(float);
+  const size_t smem = (size_t)kOmpWarps * (l_floats<TMAX>() + 32 * 32) * sizeof(float);
   auto kern = omp_batched_kernel<TMAX>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
