@@ -66,6 +66,16 @@ struct ksvd_handle {
   std::vector<cudaEvent_t> kid_events;
   cudaEvent_t fork_ev = nullptr;
   int sweep_ctas = 0;   // CTAs of this handle's cooperative sweep (0: one per SM)
+  // ksvd_iterate_host: X arrives in chunks on a copy stream; the first iteration's D'X and
+  // Batch-OMP start on each chunk as soon as its copy event fires
+  static constexpr int kMaxInflow = 16;
+  struct Inflow {
+    bool active = false;
+    int nchunks = 0;
+    int64_t bounds[kMaxInflow + 1] = {};
+    cudaEvent_t ev[kMaxInflow] = {};
+    cudaStream_t cstream = nullptr;
+  } inflow;
   int omp_grid_mult = 0;  // Batch-OMP blocks per resident CTA slot (0: default)
   int batch_chunk = 0;    // signals per batched work-queue chunk (0: default)
   int batch_concurrent = 0;  // batched updates: 1 = concurrent streams with SM shares,
@@ -285,6 +295,35 @@ ksvd_status dtx_padded(ksvd_handle* h, const float* Dp, const float* X, int64_t 
   }
   StageScope sc(h, KSVD_STAGE_DTX);
   KSVD_CK(h, launch_gemm_tn_f32(Dp, n, X, n, A0, Kp, K, Kp, N, N, n, h->stream));
+  return KSVD_OK;
+}
+
+// alpha0 columns [s0, s1) (signals s0..s1-1 of X; for the mixed path their BF16 parts are
+// made first, into the call's cached split of X).
+ksvd_status dtx_padded_range(ksvd_handle* h, const float* Dp, const float* X, int64_t N,
+                             int64_t s0, int64_t s1, float* A0) {
+  const int n = h->p.n, K = h->p.K, Kp = h->Kp;
+  const int64_t Nc = s1 - s0;
+  if (Nc <= 0) return KSVD_OK;
+  if (mixed(h)) {
+    const int64_t ld = bf16_ld(n);
+    uint16_t *hi = nullptr, *lo = nullptr;
+    int* de = nullptr;
+    KSVD_TRY(ensure(h, B_XHI, (size_t)N * ld, &hi));
+    KSVD_TRY(ensure(h, B_XLO, (size_t)N * ld, &lo));
+    KSVD_TRY(ensure(h, B_DEVERR, 1, &de));
+    StageScope sc(h, KSVD_STAGE_DTX);
+    KSVD_CK(h, launch_split_bf16(X + s0 * n, n, Nc, n, hi + s0 * ld, lo + s0 * ld, ld, Nc,
+                                 h->stream));
+    TcOperand d, x;
+    KSVD_TRY(split_dict(h, Dp, &d));
+    x.hi = hi + s0 * ld; x.lo = lo + s0 * ld; x.ld = ld; x.rows = Nc;
+    KSVD_CK(h, launch_gemm_tn_bf16(d, x, A0 + s0 * Kp, Kp, Kp, Nc, n, 3, de, h->stream));
+    return KSVD_OK;
+  }
+  StageScope sc(h, KSVD_STAGE_DTX);
+  KSVD_CK(h, launch_gemm_tn_f32(Dp, n, X + s0 * n, n, A0 + s0 * Kp, Kp, K, Kp, Nc, Nc, n,
+                                h->stream));
   return KSVD_OK;
 }
 
@@ -527,6 +566,12 @@ void ksvd_destroy(ksvd_handle* h) {
   for (auto& b : h->bufs)
     if (b.p) cudaFree(b.p);
   for (auto e : h->ev_pool) cudaEventDestroy(e);
+  if (h->inflow.cstream) {
+    cudaStreamSynchronize(h->inflow.cstream);
+    cudaStreamDestroy(h->inflow.cstream);
+  }
+  for (auto e : h->inflow.ev)
+    if (e) cudaEventDestroy(e);
   for (auto k : h->kids) ksvd_destroy(k);
   for (auto st : h->kid_streams) {
     cudaStreamSynchronize(st);
@@ -1164,8 +1209,22 @@ namespace {
 ksvd_status iteration_body(ksvd_handle* h, float* Dp, float* G, float* A0, const float* X,
                            int64_t N, int32_t* idx, float* coef, int32_t* nnz,
                            const int32_t* pd, double* rd, int32_t* cd, int* ctr) {
-  KSVD_TRY(dtx_padded(h, Dp, X, N, A0));                             // OMP.cu:44
-  KSVD_TRY(run_omp(h, G, A0, N, nullptr, nullptr, idx, coef, nnz));  // OMP.cu:55
+  if (h->inflow.active) {
+    // X is still arriving: code each chunk as soon as it has landed
+    auto& in = h->inflow;
+    in.active = false;
+    for (int c = 0; c < in.nchunks; ++c) {
+      const int64_t s0 = in.bounds[c], s1 = in.bounds[c + 1];
+      KSVD_CK(h, cudaStreamWaitEvent(h->stream, in.ev[c], 0));
+      KSVD_TRY(dtx_padded_range(h, Dp, X, N, s0, s1, A0));
+      KSVD_TRY(run_omp(h, G, A0 + s0 * h->Kp, s1 - s0, nullptr, nullptr, idx + s0 * h->p.T,
+                       coef + s0 * h->p.T, nnz + s0));
+    }
+    if (mixed(h)) { h->xsplit_src = X; h->xsplit_N = N; }   // every chunk's split is made
+  } else {
+    KSVD_TRY(dtx_padded(h, Dp, X, N, A0));                             // OMP.cu:44
+    KSVD_TRY(run_omp(h, G, A0, N, nullptr, nullptr, idx, coef, nnz));  // OMP.cu:55
+  }
   KSVD_TRY(run_update(h, Dp, X, N, idx, coef, nnz, pd, ctr));       // KSVD.cu:97-114
   KSVD_TRY(run_error(h, Dp, X, N, idx, coef, nnz, rd, ctr));        // KSVD.cu:119
   KSVD_TRY(gram_padded(h, Dp, G));                                   // G of the updated D
@@ -1318,9 +1377,37 @@ ksvd_status ksvd_iterate_host(ksvd_handle* h, float* D, const float* X, int64_t 
   KSVD_TRY(ensure(h, B_HIDX, (size_t)N * T, &dI));
   KSVD_TRY(ensure(h, B_HCOEF, (size_t)N * T, &dC));
   KSVD_TRY(ensure(h, B_HNNZ, (size_t)N, &dN));
-  KSVD_CK(h, cudaMemcpyAsync(dX, X, sizeof(float) * (size_t)n * N, cudaMemcpyHostToDevice, h->stream));
   KSVD_CK(h, cudaMemcpyAsync(dD, D, sizeof(float) * (size_t)n * K, cudaMemcpyHostToDevice, h->stream));
-  KSVD_TRY(ksvd_iterate(h, dD, dX, N, iters, perms, dI, dC, dN, rmse));
+  // X in chunks on a copy stream (after the work already queued on the handle's stream), so the
+  // first iteration's D'X and Batch-OMP overlap the rest of the transfer
+  auto& in = h->inflow;
+  const int nch = (int)std::min<int64_t>(ksvd_handle::kMaxInflow, std::max<int64_t>(1, N / 65536));
+  if (iters >= 1 && nch >= 2) {
+    if (!in.cstream) {
+      KSVD_CK(h, cudaStreamCreateWithFlags(&in.cstream, cudaStreamNonBlocking));
+      for (auto& e : in.ev) KSVD_CK(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    KSVD_CK(h, cudaEventRecord(in.ev[0], h->stream));
+    KSVD_CK(h, cudaStreamWaitEvent(in.cstream, in.ev[0], 0));
+    in.nchunks = nch;
+    for (int c = 0; c <= nch; ++c) in.bounds[c] = N * c / nch;
+    for (int c = 0; c < nch; ++c) {
+      const int64_t s0 = in.bounds[c], s1 = in.bounds[c + 1];
+      KSVD_CK(h, cudaMemcpyAsync(dX + s0 * n, X + s0 * n, sizeof(float) * (size_t)n * (s1 - s0),
+                                 cudaMemcpyHostToDevice, in.cstream));
+      KSVD_CK(h, cudaEventRecord(in.ev[c], in.cstream));
+    }
+    in.active = true;
+  } else {
+    KSVD_CK(h, cudaMemcpyAsync(dX, X, sizeof(float) * (size_t)n * N, cudaMemcpyHostToDevice,
+                               h->stream));
+  }
+  const ksvd_status st = ksvd_iterate(h, dD, dX, N, iters, perms, dI, dC, dN, rmse);
+  if (in.active) {   // not consumed (an early error): the copy must still finish before reuse
+    in.active = false;
+    cudaStreamWaitEvent(h->stream, in.ev[in.nchunks - 1], 0);
+  }
+  KSVD_TRY(st);
   KSVD_CK(h, cudaMemcpyAsync(D, dD, sizeof(float) * (size_t)n * K, cudaMemcpyDeviceToHost, h->stream));
   KSVD_CK(h, cudaMemcpyAsync(idx, dI, sizeof(int32_t) * (size_t)N * T, cudaMemcpyDeviceToHost, h->stream));
   KSVD_CK(h, cudaMemcpyAsync(coef, dC, sizeof(float) * (size_t)N * T, cudaMemcpyDeviceToHost, h->stream));

@@ -260,20 +260,26 @@ def test_iterate_matches_oracle(oracle_mod, cuda, cfg, N):
     h.close()
 
 
-def test_iterate_host_matches_device(oracle_mod, cuda):
+@pytest.mark.parametrize("N,precision", [(2000, "fp32"), (300000, "fp32"), (300000, "mixed")])
+def test_iterate_host_matches_device(oracle_mod, cuda, N, precision):
+    """ksvd_iterate_host (host arrays; from 131,072 signals X is copied in chunks on a copy
+    stream and the first iteration's D'X and Batch-OMP start on each chunk as it lands) against
+    ksvd_iterate on device-resident inputs."""
     from ksvd_gb300 import Handle, datagen, random_permutation
 
-    p = datagen.make_problem("cfg0", N=2000, dict_from="extra")
+    p = datagen.make_problem("cfg0", N=N, dict_from="extra")
     X, D = p["X"], p["D"]
     perms = np.stack([random_permutation(3, it, 256) for it in range(2)])
-    h = Handle(64, 256, 8)
+    h = Handle(64, 256, 8, precision=precision)
     Dh, ih, ch, nh, rh = h.iterate_host(D.copy(order="F"), X, 2, perms)
     Dd = to_dev(D, cuda)
     idx, coef, nnz, rd = h.iterate(Dd, to_dev(X, cuda), 2, perms)
     # the atom sweep accumulates with float atomics, so two runs agree to rounding, not bitwise
     np.testing.assert_allclose(rh, rd, rtol=1e-6)
     assert support_match_vec(ih, nh, idx.cpu().numpy(), nnz.cpu().numpy()) >= SUPPORT_MIN
-    assert rel_rmse(Dh, from_dev(Dd)) < 1e-5
+    # the sweep's float atomics reorder sums run to run; with more signals a coefficient can
+    # land on the other side of a near-tie in the second iteration's coding
+    assert rel_rmse(Dh, from_dev(Dd)) < (1e-5 if N < 100000 else 1e-3)
 
 
 def test_full_size_properties(oracle_mod, cuda):
