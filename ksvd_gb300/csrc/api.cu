@@ -75,6 +75,13 @@ struct ksvd_handle {
     int64_t bounds[kMaxInflow + 1] = {};
     cudaEvent_t ev[kMaxInflow] = {};
     cudaStream_t cstream = nullptr;
+    // results drained to the host while the last iteration finishes (ksvd_iterate_host):
+    // idx/nnz after its Batch-OMP, coef after its sweep, on cstream
+    bool drain = false;
+    int32_t* h_idx = nullptr;
+    float* h_coef = nullptr;
+    int32_t* h_nnz = nullptr;
+    cudaEvent_t dev_ev[2] = {};
   } inflow;
   int omp_grid_mult = 0;  // Batch-OMP blocks per resident CTA slot (0: default)
   int batch_chunk = 0;    // signals per batched work-queue chunk (0: default)
@@ -571,6 +578,8 @@ void ksvd_destroy(ksvd_handle* h) {
     cudaStreamDestroy(h->inflow.cstream);
   }
   for (auto e : h->inflow.ev)
+    if (e) cudaEventDestroy(e);
+  for (auto e : h->inflow.dev_ev)
     if (e) cudaEventDestroy(e);
   for (auto k : h->kids) ksvd_destroy(k);
   for (auto st : h->kid_streams) {
@@ -1225,7 +1234,25 @@ ksvd_status iteration_body(ksvd_handle* h, float* Dp, float* G, float* A0, const
     KSVD_TRY(dtx_padded(h, Dp, X, N, A0));                             // OMP.cu:44
     KSVD_TRY(run_omp(h, G, A0, N, nullptr, nullptr, idx, coef, nnz));  // OMP.cu:55
   }
+  auto& dr = h->inflow;
+  const bool drain = dr.drain;   // this is the call's last iteration and its results go to the host
+  if (drain) {
+    dr.drain = false;
+    const int T = h->p.T;
+    KSVD_CK(h, cudaEventRecord(dr.dev_ev[0], h->stream));
+    KSVD_CK(h, cudaStreamWaitEvent(dr.cstream, dr.dev_ev[0], 0));
+    KSVD_CK(h, cudaMemcpyAsync(dr.h_idx, idx, sizeof(int32_t) * (size_t)N * T,
+                               cudaMemcpyDeviceToHost, dr.cstream));
+    KSVD_CK(h, cudaMemcpyAsync(dr.h_nnz, nnz, sizeof(int32_t) * (size_t)N, cudaMemcpyDeviceToHost,
+                               dr.cstream));
+  }
   KSVD_TRY(run_update(h, Dp, X, N, idx, coef, nnz, pd, ctr));       // KSVD.cu:97-114
+  if (drain) {
+    KSVD_CK(h, cudaEventRecord(dr.dev_ev[1], h->stream));
+    KSVD_CK(h, cudaStreamWaitEvent(dr.cstream, dr.dev_ev[1], 0));
+    KSVD_CK(h, cudaMemcpyAsync(dr.h_coef, coef, sizeof(float) * (size_t)N * h->p.T,
+                               cudaMemcpyDeviceToHost, dr.cstream));
+  }
   KSVD_TRY(run_error(h, Dp, X, N, idx, coef, nnz, rd, ctr));        // KSVD.cu:119
   KSVD_TRY(gram_padded(h, Dp, G));                                   // G of the updated D
   KSVD_TRY(run_clear(h, Dp, G, X, N, cd));                           // KSVD.cu:126
@@ -1402,16 +1429,34 @@ ksvd_status ksvd_iterate_host(ksvd_handle* h, float* D, const float* X, int64_t 
     KSVD_CK(h, cudaMemcpyAsync(dX, X, sizeof(float) * (size_t)n * N, cudaMemcpyHostToDevice,
                                h->stream));
   }
+  // a single eager iteration drains its code to the host while it finishes
+  const bool drain = iters == 1 && in.cstream != nullptr;
+  if (drain) {
+    for (auto& e : in.dev_ev)
+      if (!e) KSVD_CK(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    in.drain = true;
+    in.h_idx = idx; in.h_coef = coef; in.h_nnz = nnz;
+  }
   const ksvd_status st = ksvd_iterate(h, dD, dX, N, iters, perms, dI, dC, dN, rmse);
   if (in.active) {   // not consumed (an early error): the copy must still finish before reuse
     in.active = false;
     cudaStreamWaitEvent(h->stream, in.ev[in.nchunks - 1], 0);
   }
+  const bool drained = drain && !in.drain;
+  in.drain = false;
+  if (in.cstream) {
+    // the host copies on the copy stream are complete before the call returns
+    cudaEvent_t e = in.ev[0];
+    cudaEventRecord(e, in.cstream);
+    cudaStreamWaitEvent(h->stream, e, 0);
+  }
   KSVD_TRY(st);
   KSVD_CK(h, cudaMemcpyAsync(D, dD, sizeof(float) * (size_t)n * K, cudaMemcpyDeviceToHost, h->stream));
-  KSVD_CK(h, cudaMemcpyAsync(idx, dI, sizeof(int32_t) * (size_t)N * T, cudaMemcpyDeviceToHost, h->stream));
-  KSVD_CK(h, cudaMemcpyAsync(coef, dC, sizeof(float) * (size_t)N * T, cudaMemcpyDeviceToHost, h->stream));
-  KSVD_CK(h, cudaMemcpyAsync(nnz, dN, sizeof(int32_t) * (size_t)N, cudaMemcpyDeviceToHost, h->stream));
+  if (!drained) {
+    KSVD_CK(h, cudaMemcpyAsync(idx, dI, sizeof(int32_t) * (size_t)N * T, cudaMemcpyDeviceToHost, h->stream));
+    KSVD_CK(h, cudaMemcpyAsync(coef, dC, sizeof(float) * (size_t)N * T, cudaMemcpyDeviceToHost, h->stream));
+    KSVD_CK(h, cudaMemcpyAsync(nnz, dN, sizeof(int32_t) * (size_t)N, cudaMemcpyDeviceToHost, h->stream));
+  }
   KSVD_CK(h, cudaStreamSynchronize(h->stream));
   return KSVD_OK;
 }

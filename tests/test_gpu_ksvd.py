@@ -260,20 +260,25 @@ def test_iterate_matches_oracle(oracle_mod, cuda, cfg, N):
     h.close()
 
 
-@pytest.mark.parametrize("N,precision", [(2000, "fp32"), (300000, "fp32"), (300000, "mixed")])
-def test_iterate_host_matches_device(oracle_mod, cuda, N, precision):
+@pytest.mark.parametrize("N,precision,iters", [(2000, "fp32", 2), (300000, "fp32", 2),
+                                                (300000, "mixed", 2), (300000, "fp32", 1)])
+def test_iterate_host_matches_device(oracle_mod, cuda, N, precision, iters):
     """ksvd_iterate_host (host arrays; from 131,072 signals X is copied in chunks on a copy
-    stream and the first iteration's D'X and Batch-OMP start on each chunk as it lands) against
+    stream and the first iteration's D'X and Batch-OMP start on each chunk as it lands; a
+    single-iteration call drains its code to the host while the iteration finishes) against
     ksvd_iterate on device-resident inputs."""
     from ksvd_gb300 import Handle, datagen, random_permutation
 
     p = datagen.make_problem("cfg0", N=N, dict_from="extra")
     X, D = p["X"], p["D"]
-    perms = np.stack([random_permutation(3, it, 256) for it in range(2)])
+    perms = np.stack([random_permutation(3, it, 256) for it in range(iters)])
     h = Handle(64, 256, 8, precision=precision)
-    Dh, ih, ch, nh, rh = h.iterate_host(D.copy(order="F"), X, 2, perms)
+    Dh, ih, ch, nh, rh = h.iterate_host(D.copy(order="F"), X, iters, perms)
     Dd = to_dev(D, cuda)
-    idx, coef, nnz, rd = h.iterate(Dd, to_dev(X, cuda), 2, perms)
+    idx, coef, nnz, rd = h.iterate(Dd, to_dev(X, cuda), iters, perms)
+    if iters == 1:
+        # one iteration: the drained code is the device code, up to the sweep's atomics
+        assert rel_rmse(ch, coef.cpu().numpy()) < 1e-5
     # the atom sweep accumulates with float atomics, so two runs agree to rounding, not bitwise
     np.testing.assert_allclose(rh, rd, rtol=1e-6)
     assert support_match_vec(ih, nh, idx.cpu().numpy(), nnz.cpu().numpy()) >= SUPPORT_MIN
