@@ -345,10 +345,6 @@ ksvd_status run_omp(ksvd_handle* h, const float* G, const float* A0, int64_t N,
   return KSVD_OK;
 }
 
-struct UpdateWs {
-  UpdateArgs u;
-};
-
 ksvd_status update_ws(ksvd_handle* h, int64_t N, UpdateArgs& u) {
   const int n = h->p.n, Kp = h->Kp;
   const int64_t nblk = update_block_count(N);

@@ -808,14 +808,18 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
     } else {
       // warps 8..15: d_j, G/P rows of j, the next atom's partials, prefetch; then they help
       // with the coefficients
+      // two groups of four warps in parallel (the tasks are independent: next_partials gives
+      // atom j weight 0, so it may read G/P entries refresh_gp is rewriting)
       const int gt = tid - HALF;
+      constexpr int QUART = HALF / 2;
       if (S.c == 0)
         for (int r = gt; r < n; r += HALF) A.D[(int64_t)j * n + r] = S.a_s[r] / anorm;
-      S.refresh_gp(j, 1.f / anorm, true, gt, HALF);
-      if (jn >= 0) {
-        S.next_partials(jn, j, av_next, ad_next, gt, HALF);
-        S.zero_row(jn, gt, HALF);
-        S.prefetch_next(jn, (jj + 1) & 1, gt, HALF);
+      if (gt < QUART) {
+        S.refresh_gp(j, 1.f / anorm, true, gt, QUART);
+      } else if (jn >= 0) {
+        S.next_partials(jn, j, av_next, ad_next, gt - QUART, QUART);
+        S.zero_row(jn, gt - QUART, QUART);
+        S.prefetch_next(jn, (jj + 1) & 1, gt - QUART, QUART);
       }
       S.update_coefs(j, q0, cnt, anorm, jj & 1, &next_batch, &use_cnt);
     }

@@ -421,3 +421,31 @@ def test_reference_recorded_dictionary_thirty_iterations(oracle_mod, cuda):
     assert G.shape == (N, K)
     assert np.all((G != 0).sum(axis=1) == T)
     h.close()
+
+
+def test_ksvd_object_stages_match_execute_iterations(cuda):
+    """The reference's object model (KSVD.cuh:21-27): normcols, batch_omp, update_dictionary,
+    error_computation and clear_dict called one by one give the same iteration as
+    execute_iterations(1) with the same atom order."""
+    import torch
+
+    from ksvd_gb300 import KSVD, datagen, random_permutation
+
+    p = datagen.make_problem("cfg0", N=5000, dict_from="extra")
+    X = torch.from_numpy(np.ascontiguousarray(np.asarray(p["X"], np.float32).T)).to(cuda)
+    D = torch.from_numpy(np.ascontiguousarray(np.asarray(p["D"], np.float32).T)).to(cuda)
+    perm = random_permutation(5, 0, 256)
+    a = KSVD(X, D, 8)
+    a.normcols()
+    a.batch_omp()
+    a.update_dictionary(perm)
+    ra = a.error_computation()
+    a.clear_dict()
+    b = KSVD(X, D, 8)
+    rb = b.execute_iterations(1, perms=perm[None, :])
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(ra, rb[0], rtol=1e-5)
+    assert rel_rmse(a.D.cpu().numpy(), b.D.cpu().numpy()) < 1e-4
+    assert (a.idx == b.idx).float().mean().item() >= 0.999
+    G = b.dense_gamma()
+    assert G.shape == (5000, 256) and int((G != 0).sum(1).max()) <= 8
