@@ -292,6 +292,13 @@ KSVD_API ksvd_status ksvd_iterate(ksvd_handle* handle, float* D, const float* X,
                          const int32_t* perms, int32_t* idx, float* coef, int32_t* nnz,
                          double* rmse);
 
+/* ksvd_iterate with error-constrained coding: signal s stops taking atoms once
+ * ||x_s - D gamma_s||^2 <= eps2[s] (device, N floats) or after T atoms (Rubinstein et al.'s
+ * Batch-OMP stopping rule; the reference codes to sparsity T only). */
+KSVD_API ksvd_status ksvd_iterate_eps(ksvd_handle* handle, float* D, const float* X, int64_t N,
+                                      int32_t iters, const int32_t* perms, const float* eps2,
+                                      int32_t* idx, float* coef, int32_t* nnz, double* rmse);
+
 /* Same as ksvd_iterate with every array in HOST memory: X and D are copied to the device, the
  * iterations run, and D, idx, coef, nnz are copied back.  This is the whole-program contract of
  * the reference executable (main.cu:42-159) minus its MAT-file I/O. */

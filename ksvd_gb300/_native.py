@@ -34,6 +34,7 @@ EXPORTS = (
     "ksvd_refine_coefs", "ksvd_batched_omp", "ksvd_graph_replays",
     "ksvd_batched_iterate", "ksvd_remove_row_mean", "ksvd_perm_draws", "ksvd_set_perm_draws",
     "ksvd_autotune", "ksvd_autotune_batched", "ksvd_get_tuning", "ksvd_set_tuning",
+    "ksvd_iterate_eps",
 )
 
 FLAG_PROFILE = 1
@@ -124,6 +125,7 @@ def _declare(lib):
         "ksvd_autotune_batched": (st, [vp, vp, i32, vp]),
         "ksvd_get_tuning": (st, [vp, vp]),
         "ksvd_set_tuning": (st, [vp, vp]),
+        "ksvd_iterate_eps": (st, [vp, vp, vp, i64, i32, vp, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -249,8 +249,9 @@ class Handle:
                                               _ptr(coef), _ptr(nnz), C.byref(c)))
         return int(c.value)
 
-    def iterate(self, D, X, iters, perms=None, out=None):
-        """iters K-SVD iterations on device tensors; D is updated in place.
+    def iterate(self, D, X, iters, perms=None, out=None, eps2=None):
+        """iters K-SVD iterations on device tensors; D is updated in place.  eps2 (N,) float32
+        device tensor: error-constrained coding (||x - D gamma||^2 <= eps2, at most T atoms).
         Returns (idx, coef, nnz, rmse[iters])."""
         import torch
 
@@ -265,9 +266,15 @@ class Handle:
             if perms.shape != (iters, self.K):
                 raise ValueError("perms must be (iters, K)")
             pp = perms.ctypes.data_as(C.c_void_p)
-        self._check(self._lib.ksvd_iterate(self._h, _ptr(D), _ptr(X), N, int(iters), pp,
-                                           _ptr(idx), _ptr(coef), _ptr(nnz),
-                                           rmse.ctypes.data_as(C.c_void_p)))
+        if eps2 is not None:
+            _need(eps2, "eps2", torch.float32, (N,))
+            self._check(self._lib.ksvd_iterate_eps(self._h, _ptr(D), _ptr(X), N, int(iters), pp,
+                                                   _ptr(eps2), _ptr(idx), _ptr(coef), _ptr(nnz),
+                                                   rmse.ctypes.data_as(C.c_void_p)))
+        else:
+            self._check(self._lib.ksvd_iterate(self._h, _ptr(D), _ptr(X), N, int(iters), pp,
+                                               _ptr(idx), _ptr(coef), _ptr(nnz),
+                                               rmse.ctypes.data_as(C.c_void_p)))
         return idx, coef, nnz, rmse[:iters]
 
     def iterate_host(self, D, X, iters, perms=None, out=None):

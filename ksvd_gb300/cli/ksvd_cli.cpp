@@ -9,7 +9,8 @@
 //   then rows x cols values, column-major, little-endian.
 //
 //   ksvd [options] X.raw D.raw Gamma.raw [Dout.raw]
-//     -T t                 atoms per signal (required)
+//     -T t                 atoms per signal (required; with --eps, the most per signal)
+//     --eps E              error-constrained coding: a signal stops once ||x - D gamma|| <= E
 //     --iters N            K-SVD iterations (default 10)
 //     --precision P        fp32 | mixed (default fp32)
 //     --seed S             atom-order seed (default 0x4B535644)
@@ -119,7 +120,8 @@ bool read_checkpoint(const char* path, int32_t n, int32_t K, int32_t* done, uint
 void usage() {
   std::printf(
       "usage: ksvd [options] X.raw D.raw Gamma.raw [Dout.raw]\n"
-      "  -T t                 atoms per signal (required)\n"
+      "  -T t                 atoms per signal (required; with --eps, the most per signal)\n"
+      "  --eps E              error-constrained coding: stop once ||x - D gamma|| <= E\n"
       "  --iters N            K-SVD iterations (default 10)\n"
       "  --precision P        fp32 | mixed (default fp32)\n"
       "  --seed S             atom-order seed (default 0x4B535644)\n"
@@ -154,6 +156,7 @@ void usage() {
 
 int main(int argc, char** argv) {
   int T = 0, iters = 10, every = 0;
+  double eps = -1.0;
   int precision = KSVD_PREC_FP32;
   uint64_t seed = 0x4B535644ULL;
   bool remove_mean = false, refine = false, graph = false;
@@ -166,6 +169,7 @@ int main(int argc, char** argv) {
     if (a == "-h" || a == "--help") { usage(); return 0; }
     else if (a == "-T" && (v = next())) T = std::atoi(v);
     else if (a == "--iters" && (v = next())) iters = std::atoi(v);
+    else if (a == "--eps" && (v = next())) eps = std::atof(v);
     else if (a == "--precision" && (v = next()))
       precision = std::string(v) == "mixed" ? KSVD_PREC_MIXED : KSVD_PREC_FP32;
     else if (a == "--seed" && (v = next())) seed = std::strtoull(v, nullptr, 0);
@@ -208,7 +212,7 @@ int main(int argc, char** argv) {
   CUDA_OR_DIE(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
   KSVD_OR_DIE(h, ksvd_create(&h, &p, st));
   KSVD_OR_DIE(h, ksvd_set_perm_draws(h, draws));
-  float *dX = nullptr, *dD = nullptr, *dC = nullptr, *dG = nullptr;
+  float *dX = nullptr, *dD = nullptr, *dC = nullptr, *dG = nullptr, *dE = nullptr;
   int32_t *dI = nullptr, *dN = nullptr;
   CUDA_OR_DIE(cudaMalloc(&dX, sizeof(float) * X.v.size()));
   CUDA_OR_DIE(cudaMalloc(&dD, sizeof(float) * D.v.size()));
@@ -218,6 +222,11 @@ int main(int argc, char** argv) {
   CUDA_OR_DIE(cudaMemcpyAsync(dX, X.v.data(), sizeof(float) * X.v.size(), cudaMemcpyHostToDevice, st));
   CUDA_OR_DIE(cudaMemcpyAsync(dD, D.v.data(), sizeof(float) * D.v.size(), cudaMemcpyHostToDevice, st));
   if (remove_mean) KSVD_OR_DIE(h, ksvd_remove_row_mean(h, dX, N, nullptr));
+  if (eps >= 0) {
+    std::vector<float> e2((size_t)N, (float)(eps * eps));
+    CUDA_OR_DIE(cudaMalloc(&dE, sizeof(float) * (size_t)N));
+    CUDA_OR_DIE(cudaMemcpy(dE, e2.data(), sizeof(float) * e2.size(), cudaMemcpyHostToDevice));
+  }
   std::printf("Running...\n\n");
 
   cudaEvent_t e0, e1;
@@ -228,7 +237,10 @@ int main(int argc, char** argv) {
   std::vector<double> rmse(chunk > 0 ? chunk : 1);
   for (int it = done; it < iters;) {
     const int m = std::min(chunk, iters - it);
-    KSVD_OR_DIE(h, ksvd_iterate(h, dD, dX, N, m, nullptr, dI, dC, dN, rmse.data()));
+    if (dE)
+      KSVD_OR_DIE(h, ksvd_iterate_eps(h, dD, dX, N, m, nullptr, dE, dI, dC, dN, rmse.data()));
+    else
+      KSVD_OR_DIE(h, ksvd_iterate(h, dD, dX, N, m, nullptr, dI, dC, dN, rmse.data()));
     for (int k = 0; k < m; ++k)
       std::printf("Iteration %02d / %d complete, RMSE = %.5f\n", it + k + 1, iters, rmse[k]);
     it += m;
@@ -277,6 +289,7 @@ int main(int argc, char** argv) {
   std::printf("Memory Utilization =>\t\t%.1f %%\n", 100.0 * used_prog / (double)total);
   ksvd_destroy(h);
   cudaFree(dX); cudaFree(dD); cudaFree(dI); cudaFree(dC); cudaFree(dN); cudaFree(dG);
+  if (dE) cudaFree(dE);
   cudaStreamDestroy(st);
   std::printf("----------------------------------------------------\n# Exiting!\n");
   return 0;

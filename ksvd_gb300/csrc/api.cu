@@ -47,10 +47,10 @@ struct ksvd_handle {
   bool profiling() const { return (p.flags & KSVD_FLAG_PROFILE) != 0; }
   // CUDA graph of one K-SVD iteration (KSVD_FLAG_GRAPH): captured on a side stream, replayed
   struct GraphKey {
-    const void* p[12];
+    const void* p[13];
     int64_t N;
     bool operator==(const GraphKey& o) const {
-      for (int i = 0; i < 12; ++i) if (p[i] != o.p[i]) return false;
+      for (int i = 0; i < 13; ++i) if (p[i] != o.p[i]) return false;
       return N == o.N;
     }
   };
@@ -66,6 +66,9 @@ struct ksvd_handle {
   std::vector<cudaEvent_t> kid_events;
   cudaEvent_t fork_ev = nullptr;
   int sweep_ctas = 0;   // CTAs of this handle's cooperative sweep (0: one per SM)
+  // error-constrained iterations (ksvd_iterate_eps): per-signal ||x||^2 and targets, for the call
+  const float* it_xn2 = nullptr;
+  const float* it_eps2 = nullptr;
   // ksvd_iterate_host: X arrives in chunks on a copy stream; the first iteration's D'X and
   // Batch-OMP start on each chunk as soon as its copy event fires
   static constexpr int kMaxInflow = 16;
@@ -1222,13 +1225,17 @@ ksvd_status iteration_body(ksvd_handle* h, float* Dp, float* G, float* A0, const
       const int64_t s0 = in.bounds[c], s1 = in.bounds[c + 1];
       KSVD_CK(h, cudaStreamWaitEvent(h->stream, in.ev[c], 0));
       KSVD_TRY(dtx_padded_range(h, Dp, X, N, s0, s1, A0));
-      KSVD_TRY(run_omp(h, G, A0 + s0 * h->Kp, s1 - s0, nullptr, nullptr, idx + s0 * h->p.T,
+      if (h->it_eps2)
+        KSVD_CK(h, launch_col_norm2(X + s0 * h->p.n, h->p.n, s1 - s0,
+                                    const_cast<float*>(h->it_xn2) + s0, h->stream));
+      KSVD_TRY(run_omp(h, G, A0 + s0 * h->Kp, s1 - s0, h->it_eps2 ? h->it_xn2 + s0 : nullptr,
+                       h->it_eps2 ? h->it_eps2 + s0 : nullptr, idx + s0 * h->p.T,
                        coef + s0 * h->p.T, nnz + s0));
     }
     if (mixed(h)) { h->xsplit_src = X; h->xsplit_N = N; }   // every chunk's split is made
   } else {
     KSVD_TRY(dtx_padded(h, Dp, X, N, A0));                             // OMP.cu:44
-    KSVD_TRY(run_omp(h, G, A0, N, nullptr, nullptr, idx, coef, nnz));  // OMP.cu:55
+    KSVD_TRY(run_omp(h, G, A0, N, h->it_xn2, h->it_eps2, idx, coef, nnz));  // OMP.cu:55
   }
   auto& dr = h->inflow;
   const bool drain = dr.drain;   // this is the call's last iteration and its results go to the host
@@ -1327,12 +1334,40 @@ bool replay_graph(ksvd_handle* h, const ksvd_handle::GraphKey& key, int32_t coun
 
 }  // namespace
 
+namespace {
+ksvd_status iterate_impl(ksvd_handle* h, float* D, const float* X, int64_t N, int32_t iters,
+                         const int32_t* perms, const float* eps2, int32_t* idx, float* coef,
+                         int32_t* nnz, double* rmse);
+}
+
 ksvd_status ksvd_iterate(ksvd_handle* h, float* D, const float* X, int64_t N, int32_t iters,
                          const int32_t* perms, int32_t* idx, float* coef, int32_t* nnz,
                          double* rmse) {
+  return iterate_impl(h, D, X, N, iters, perms, nullptr, idx, coef, nnz, rmse);
+}
+
+ksvd_status ksvd_iterate_eps(ksvd_handle* h, float* D, const float* X, int64_t N, int32_t iters,
+                             const int32_t* perms, const float* eps2, int32_t* idx, float* coef,
+                             int32_t* nnz, double* rmse) {
+  if (bad_ptr(eps2)) return KSVD_ERR_INVALID_ARGUMENT;
+  return iterate_impl(h, D, X, N, iters, perms, eps2, idx, coef, nnz, rmse);
+}
+
+namespace {
+// The call's error targets live in the handle while it runs (the iteration body and a captured
+// graph read them from there); cleared on every exit.
+struct EpsScope {
+  ksvd_handle* h;
+  ~EpsScope() { h->it_xn2 = nullptr; h->it_eps2 = nullptr; }
+};
+
+ksvd_status iterate_impl(ksvd_handle* h, float* D, const float* X, int64_t N, int32_t iters,
+                         const int32_t* perms, const float* eps2, int32_t* idx, float* coef,
+                         int32_t* nnz, double* rmse) {
   if (!h || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || N < 1 ||
       iters < 0)
     return KSVD_ERR_INVALID_ARGUMENT;
+  EpsScope eps_scope{h};
   if (iters > 1024) return fail(h, KSVD_ERR_UNSUPPORTED, "at most 1024 iterations per call%s");
   if ((int64_t)N * h->p.T > 0x7fffffffLL)
     return fail(h, KSVD_ERR_UNSUPPORTED, "N*T must stay below 2^31%s");
@@ -1352,6 +1387,13 @@ ksvd_status ksvd_iterate(ksvd_handle* h, float* D, const float* X, int64_t N, in
   KSVD_TRY(ensure(h, B_CLEARED, 1, &cd));
   KSVD_TRY(ensure(h, B_ITER, 1, &ctr));
   KSVD_CK(h, cudaMemsetAsync(ctr, 0, sizeof(int), h->stream));
+  if (eps2) {
+    float* xn2 = nullptr;
+    KSVD_TRY(ensure(h, B_XN2, (size_t)N, &xn2));
+    if (!h->inflow.active) KSVD_CK(h, launch_col_norm2(X, h->p.n, N, xn2, h->stream));
+    h->it_xn2 = xn2;          // (with X still arriving, per chunk in the first iteration)
+    h->it_eps2 = eps2;
+  }
   if (iters > 0) KSVD_TRY(upload_perm(h, perms, iters, &pd));
   KSVD_CK(h, launch_normcols(Dp, h->p.n, h->p.K, h->stream));         // KSVD.cu:57
   KSVD_TRY(gram_padded(h, Dp, G));                                     // KSVD.cu:64
@@ -1364,7 +1406,8 @@ ksvd_status ksvd_iterate(ksvd_handle* h, float* D, const float* X, int64_t N, in
   }
   if (graph && done < iters) {
     ksvd_handle::GraphKey key{{Dp, G, A0, X, idx, coef, nnz, pd, rd, cd, ctr,
-                               reinterpret_cast<const void*>((intptr_t)h->p.precision)},
+                               reinterpret_cast<const void*>((intptr_t)h->p.precision),
+                               h->it_eps2},
                               N};
     if (replay_graph(h, key, iters - done, Dp, G, A0, X, N, idx, coef, nnz, pd, rd, cd, ctr))
       done = iters;
@@ -1386,6 +1429,7 @@ ksvd_status ksvd_iterate(ksvd_handle* h, float* D, const float* X, int64_t N, in
   collect_stage_times(h);
   return check_dev_err(h);
 }
+}  // namespace
 
 ksvd_status ksvd_iterate_host(ksvd_handle* h, float* D, const float* X, int64_t N, int32_t iters,
                               const int32_t* perms, int32_t* idx, float* coef, int32_t* nnz,

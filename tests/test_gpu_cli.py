@@ -90,3 +90,20 @@ def test_remove_row_mean(cuda):
                                X.astype(np.float32).astype(np.float64).mean(axis=1), rtol=1e-6)
     assert np.abs(want.mean(axis=0)).max() <= 1e-5
     h.close()
+
+
+def test_cli_error_target(cuda, tmp_path):
+    """--eps: error-constrained coding through the CLI; every signal's code meets the target or
+    uses T atoms."""
+    from ksvd_gb300 import matio
+
+    p = _files(tmp_path)
+    X = np.asarray(p["X"], np.float64)
+    eps = float(0.3 * np.median(np.linalg.norm(X, axis=0)))
+    out = _run(["-T", 20, "--eps", eps, "--iters", 2, tmp_path / "X.raw", tmp_path / "D.raw",
+                tmp_path / "G.raw", tmp_path / "Dout.raw"])
+    assert len(RMSE_LINE.findall(out)) == 2
+    G = matio.read_raw(tmp_path / "G.raw")
+    D = matio.read_raw(tmp_path / "Dout.raw")
+    counts = (G != 0).sum(axis=0)
+    assert counts.max() <= 20 and counts.mean() < 20

@@ -449,3 +449,41 @@ def test_ksvd_object_stages_match_execute_iterations(cuda):
     assert (a.idx == b.idx).float().mean().item() >= 0.999
     G = b.dense_gamma()
     assert G.shape == (5000, 256) and int((G != 0).sum(1).max()) <= 8
+
+
+def test_iterate_error_constrained_matches_oracle(oracle_mod, cuda):
+    """ksvd_iterate_eps: K-SVD iterations with error-constrained coding (a signal stops taking
+    atoms once ||x - D gamma||^2 <= eps2, at most T), against the oracle's stages composed the
+    same way (normcols once; per iteration Gram, error-constrained Batch-OMP, sweep, error,
+    clearDict): first-iteration supports >= 99.9%, RMSE of two iterations within 1e-3."""
+    import torch
+
+    from ksvd_gb300 import Handle, datagen, random_permutation
+
+    p = datagen.make_problem("cfg0", N=3000, dict_from="extra")
+    X, D = p["X"].astype(np.float64), p["D"].astype(np.float64)
+    n, K, T = 64, 256, 12
+    xn2 = np.sum(X * X, 0)
+    e2 = (0.08 * xn2).astype(np.float32)
+    perms = np.stack([random_permutation(9, it, K) for it in range(2)])
+    D64 = oracle_mod.normcols(np.asfortranarray(D))
+    rr, first = [], None
+    for it in range(2):
+        idx, coef, nnz = oracle_mod.omp(oracle_mod.gram(D64), oracle_mod.dtx(D64, X), T,
+                                        xnorm2=xn2, eps2=e2.astype(np.float64))
+        if first is None:
+            first = (idx, nnz)
+        D64, coef, st = oracle_mod.update(X, D64, idx, coef, nnz, perms[it])
+        r, err = oracle_mod.error(X, D64, idx, coef, nnz, st["bitmap"])
+        rr.append(r)
+        D64, _, _ = oracle_mod.cleardict(X, D64, idx, coef, nnz, st["replaced"], err)
+    h = Handle(n, K, T)
+    Xd = to_dev(X.astype(np.float32), cuda)
+    e2d = torch.from_numpy(e2).to(cuda)
+    gi, gc, gn, r1 = h.iterate(to_dev(D.astype(np.float32), cuda), Xd, 1, perms[:1], eps2=e2d)
+    assert support_match_vec(gi.cpu().numpy(), gn.cpu().numpy(), *first) >= SUPPORT_MIN
+    assert gn.cpu().numpy().min() >= 1 and gn.cpu().numpy().max() <= T
+    _, _, gn2, r2 = h.iterate(to_dev(D.astype(np.float32), cuda), Xd, 2, perms, eps2=e2d)
+    np.testing.assert_allclose(r2, rr, rtol=1e-3)
+    assert float(gn2.float().mean()) < T            # the targets, not T, ended most codes
+    h.close()
