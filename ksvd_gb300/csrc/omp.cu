@@ -35,6 +35,15 @@ __device__ __forceinline__ int lidx(int r, int q) {
   else return r * (TMAX + 1) + q;
 }
 
+// 16-byte read-only load that does not allocate in L1
+__device__ __forceinline__ float4 ldg_f4_no_l1(const float* p) {
+  float4 g;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
+               : "=f"(g.x), "=f"(g.y), "=f"(g.z), "=f"(g.w)
+               : "l"(p));
+  return g;
+}
+
 template <int SPL>
 __device__ __forceinline__ float pick(const float (&a)[SPL], int j) {
   if constexpr (SPL == 1) return a[0];
@@ -182,7 +191,9 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G, int64_t 
         for (int m = 0; m < M4; ++m)
 #pragma unroll
           for (int q = 0; q < 4; ++q) al[m][q] = 0.f;
-#pragma unroll 2
+        // one support column per step (deeper unrolling measured slower: register pressure);
+        // G's columns bypass L1 allocation -- they are reused from L2, not from L1
+#pragma unroll 1
         for (int r = 0; r < i; ++r) {
           const int rl = r & 31, rj = r >> 5;
           const float cr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(c, rj), rl);
@@ -190,7 +201,7 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G, int64_t 
           const float* gp = G + (int64_t)col * ldg + 4 * lane;
 #pragma unroll
           for (int m = 0; m < M4; ++m) {
-            const float4 g = __ldg(reinterpret_cast<const float4*>(gp + 128 * m));
+            const float4 g = ldg_f4_no_l1(gp + 128 * m);
             al[m][0] = fmaf(g.x, cr, al[m][0]);
             al[m][1] = fmaf(g.y, cr, al[m][1]);
             al[m][2] = fmaf(g.z, cr, al[m][2]);

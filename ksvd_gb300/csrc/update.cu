@@ -296,13 +296,16 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
   return v;
 }
 
-// L2 prefetch of every 128-byte line of [p, p + bytes), one fire-and-forget instruction per line
-// through the load/store path (bulk prefetches would queue on the SM's single TMA unit).
+// Brings every 128-byte line of [p, p + bytes) into L2: one L2-only load per line whose value is
+// never used (nothing waits for it).  Measured better than prefetch.global.L2, which the memory
+// system may drop, and than bulk prefetches, which queue on the SM's single TMA unit.
 __device__ __forceinline__ void prefetch_l2_lines(const void* p, uint32_t bytes) {
   const uintptr_t a0 = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(127);
   const uintptr_t a1 = reinterpret_cast<uintptr_t>(p) + bytes;
-  for (uintptr_t a = a0; a < a1; a += 128)
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(a) : "memory");
+  for (uintptr_t a = a0; a < a1; a += 128) {
+    unsigned v;
+    asm volatile("ld.global.cg.b32 %0, [%1];" : "=r"(v) : "l"(a) : "memory");
+  }
 }
 
 // Generation barrier over all CTAs of the cooperative launch.  Bounded: returns false (and
