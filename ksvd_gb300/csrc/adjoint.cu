@@ -101,6 +101,7 @@ code_fixed_kernel(const float* __restrict__ D, int n, int K, const float* __rest
       const int i = e / t, j = e - i * t;
       if (j <= i && okidx) L[i * LS + j] = G[(int64_t)at[j] * ldg + at[i]];
     }
+    #pragma unroll 4
     for (int j = 0; j < t; ++j) {
       float acc = 0.f;
       if (okidx) {
@@ -172,6 +173,7 @@ code_backward_kernel(const float* __restrict__ D, int n, int K, const float* __r
       au[i] = 0.f;
     }
     if (ok) {
+      #pragma unroll 4
       for (int j = 0; j < t; ++j) {
         const float* d = D + (int64_t)at[j] * n;
         const float gj = coef[s * T + j], uj = u[j];
@@ -193,6 +195,7 @@ code_backward_kernel(const float* __restrict__ D, int n, int K, const float* __r
       if (dx && rr < n) dx[rr] = ok ? au[i] : 0.f;
     }
     if (ok && dD) {
+      #pragma unroll 4
       for (int j = 0; j < t; ++j) {
         float* dd = dD + (int64_t)at[j] * n;
         const float gj = coef[s * T + j], uj = u[j];
@@ -242,6 +245,7 @@ refine_kernel(const float* __restrict__ D, int n, int K, const float* __restrict
       r[i] = rr < n ? (double)x[rr] : 0.0;
     }
     if (okidx)
+      #pragma unroll 4
       for (int j = 0; j < t; ++j) {
         const float* d = D + (int64_t)at[j] * n;
         const double gj = (double)coef[s * T + j];
@@ -257,6 +261,7 @@ refine_kernel(const float* __restrict__ D, int n, int K, const float* __restrict
     }
     // b = A'r in FP64 too: r is nearly orthogonal to the support columns, so an FP32 sum would
     // lose the small result to cancellation (error ~2^-24 ||r|| instead of ~2^-24 |b|)
+    #pragma unroll 4
     for (int j = 0; j < t; ++j) {
       double acc = 0.0;
       if (okidx) {

@@ -41,11 +41,24 @@ error_kernel(ErrorArgs A) {
       const int r = lane + 32 * i;
       acc[i] = r < n ? __ldcs(x + r) : 0.f;
     }
+    // the whole code row in registers first (lane t holds slots t and t + 32), so the support
+    // columns' loads do not wait on one another
     const int nz = min(A.nnz[s], T);
+    int kk[2];
+    float gg[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int t = lane + 32 * u;
+      const int k = t < nz ? A.idx[s * T + t] : -1;
+      const bool ok = k >= 0 && k < A.K;
+      kk[u] = ok ? k : -1;
+      gg[u] = ok ? A.coef[s * T + t] : 0.f;
+    }
+#pragma unroll 4
     for (int t = 0; t < nz; ++t) {
-      const int k = A.idx[s * T + t];
-      if (k < 0 || k >= A.K) continue;
-      const float g = A.coef[s * T + t];
+      const int k = __shfl_sync(KSVD_FULL_MASK, (t >> 5) == 0 ? kk[0] : kk[1], t & 31);
+      const float g = __shfl_sync(KSVD_FULL_MASK, (t >> 5) == 0 ? gg[0] : gg[1], t & 31);
+      if (k < 0) continue;
       const float* d = A.D + (int64_t)k * n;
 #pragma unroll
       for (int i = 0; i < NPL; ++i) {

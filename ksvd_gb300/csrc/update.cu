@@ -175,7 +175,9 @@ prepare_kernel(const float* __restrict__ X, int n, int T, int Kp, const int32_t*
 #pragma unroll
   for (int i = 0; i < NPL; ++i) acc[i] = 0.f;
   float g2 = 0.f;
-  constexpr int EB = NPL <= 8 ? 4 : (NPL <= 16 ? 2 : 1);      // entries in flight per warp
+  // entries per warp batch: 2 keeps the kernel at <= 64 registers, two 512-thread CTAs per SM
+  // (measured faster than 4 or 6 entries with one CTA per SM)
+  constexpr int EB = NPL <= 16 ? 2 : 1;
   // the list entries of the warp's next batch are loaded one batch ahead, so each batch costs
   // one round of loads (signals and code rows) instead of two
   int32_t ecur[EB];
