@@ -219,7 +219,11 @@ def run_reference(args, cfg):
     return 0
 
 
-def cpu_baseline(cfg, sample, reps=1):
+def cpu_baseline(cfg, sample, reps=1, check_iters=3, check_signals=20000):
+    """The oracle on the host cores: one K-SVD iteration on a sample of the workload, timed and
+    scaled by N.  Also returns the FP64 oracle's per-iteration RMSE over `check_iters`
+    iterations of the first `check_signals` signals of that sample with fixed atom orders, for
+    the GPU path to be compared with on the same signals (the check, not a timing)."""
     import numpy as np
 
     import oracle
@@ -235,10 +239,39 @@ def cpu_baseline(cfg, sample, reps=1):
         oracle.ksvd(p["X"], p["D"], cfg.T, 1, perm)
         ts.append(time.perf_counter() - t0)
     t = statistics.median(ts)
-    return {"value": 1.0 / (t * cfg.N / Ns), "unit": "iter/s", "cores": oracle.num_threads(),
+    base = {"value": 1.0 / (t * cfg.N / Ns), "unit": "iter/s", "cores": oracle.num_threads(),
             "kind": "port",
             "sample": "one K-SVD iteration on %d of %d signals (%.2f s), scaled by N" %
                       (Ns, cfg.N, t)}
+    check = None
+    if check_iters > 0:
+        rng = np.random.default_rng(1)
+        perms = np.stack([rng.permutation(cfg.K) for _ in range(check_iters)]).astype(np.int32)
+        Xc = np.asfortranarray(p["X"][:, :min(Ns, check_signals)])
+        r64 = oracle.ksvd(Xc.astype(np.float64), p["D"].astype(np.float64), cfg.T,
+                          check_iters, perms)[4]
+        check = dict(X=Xc, D=p["D"], perms=perms, rmse_fp64=[float(v) for v in r64])
+    return base, check
+
+
+def error_vs_fp64(cfg, check, precision, device):
+    """Per-iteration RMSE of the GPU path on the oracle check's sample (same data, initial
+    dictionary and atom orders) beside the FP64 oracle's."""
+    import numpy as np
+    import torch
+
+    from ksvd_gb300 import Handle
+
+    X = torch.from_numpy(np.ascontiguousarray(check["X"].T)).to(device)
+    D = torch.from_numpy(np.ascontiguousarray(check["D"].T)).to(device)
+    iters = check["perms"].shape[0]
+    h = Handle(cfg.n, cfg.K, cfg.T, precision=precision)
+    rg = [float(v) for v in h.iterate(D, X, iters, perms=check["perms"])[3]]
+    h.close()
+    r64 = check["rmse_fp64"]
+    return {"sample_signals": int(X.shape[0]), "iterations": iters,
+            "rmse_gpu": rg, "rmse_fp64_oracle": r64,
+            "rel_diff_per_iter": [abs(a - b) / b for a, b in zip(rg, r64)]}
 
 
 def cpu_baseline_batched(probs, per_problem):
@@ -480,9 +513,9 @@ def main():
     from ksvd_gb300 import Handle
 
     # CPU baseline first (before any CUDA work in this process), rank 0 at N=1 only
-    cpu = None
+    cpu = check = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        cpu = cpu_baseline(cfg, args.cpu_sample)
+        cpu, check = cpu_baseline(cfg, args.cpu_sample)
 
     prob = datagen.make_problem(cfg, N=args.signals,
                                 seed=datagen.SEED_BASE + cfg.index + 1000 * rank, device="cuda")
@@ -541,6 +574,9 @@ def main():
                     "rmse_max_rel_diff": max(abs(a - b) / b for a, b in zip(rms, rf)),
                     "rmse_per_iter_mixed": rms, "rmse_per_iter_fp32": rf}
         hf.close()
+    fp64_check = None
+    if check is not None:
+        fp64_check = error_vs_fp64(cfg, check, args.precision, dev)
     hp.iterate(D, X, 1, out=out)                  # warm the profiling handle's workspace
     hp.stage_times(reset=True)
     hp.iterate(D, X, min(args.steps, 5), out=out)
@@ -639,6 +675,7 @@ def main():
             args.steps * KERNELS_PER_ITER[args.precision],
             "clocks": clocks,
             "rmse_last": rms[-1] if rms else None,
+            "error_vs_fp64_oracle": fp64_check,
             "wall_s_timed": t_wall,
         }
         print(json.dumps(line), flush=True)

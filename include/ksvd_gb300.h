@@ -215,8 +215,9 @@ KSVD_API ksvd_status ksvd_code_backward(ksvd_handle* handle, const float* D, con
                                         const float* coef, const float* chol, const float* dcoef,
                                         float* dD, float* dX);
 
-/* Number of iterations ksvd_iterate has run as CUDA-graph replays on this handle (0 when the
- * flag is off or capture was refused, in which case the iterations ran as plain launches). */
+/* Number of iterations ksvd_iterate and ksvd_batched_iterate have run as CUDA-graph replays on
+ * this handle (0 when the flag is off or capture was refused, in which case the iterations ran
+ * as plain launches). */
 KSVD_API int64_t ksvd_graph_replays(const ksvd_handle* handle);
 
 /* ---- autotuning --------------------------------------------------------------------------- */
@@ -277,6 +278,8 @@ KSVD_API ksvd_status ksvd_batched_omp(ksvd_handle* handle, const ksvd_problem* p
  * SMs in proportion to N*T.  D is normalised first and updated in place; idx/coef/nnz hold the last
  * iteration's code; rmse (host, nullable) gets nprob x iters values, problem-major.  The
  * handle's mu_thresh, use_thresh, max_replace_signals and seed apply to every problem (FP32).
+ * With KSVD_FLAG_GRAPH on the handle, iterations 2..iters replay one CUDA graph of the whole
+ * batched iteration (captured once per set of buffers and shapes).
  * Replaces a host loop of KSVD::ExecuteIterations calls (S/KSVD.cu:55-131), one per dictionary. */
 KSVD_API ksvd_status ksvd_batched_iterate(ksvd_handle* handle, ksvd_problem* probs,
                                           int32_t nprob, int32_t iters, double* rmse);

@@ -154,7 +154,7 @@ class Handle:
         self._check(self._lib.ksvd_set_tuning(self._h, C.byref(t)))
 
     def graph_replays(self) -> int:
-        """Iterations ksvd_iterate ran as CUDA-graph replays on this handle."""
+        """Iterations ksvd_iterate / ksvd_batched_iterate ran as CUDA-graph replays."""
         return int(self._lib.ksvd_graph_replays(self._h))
 
     def stage_times(self, reset=False):

@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -45,19 +46,16 @@ struct ksvd_handle {
   double stage_ms[8] = {0};
   int64_t stage_calls[8] = {0};
   bool profiling() const { return (p.flags & KSVD_FLAG_PROFILE) != 0; }
-  // CUDA graph of one K-SVD iteration (KSVD_FLAG_GRAPH): captured on a side stream, replayed
-  struct GraphKey {
-    const void* p[13];
-    int64_t N;
-    bool operator==(const GraphKey& o) const {
-      for (int i = 0; i < 13; ++i) if (p[i] != o.p[i]) return false;
-      return N == o.N;
-    }
+  // CUDA graphs of one K-SVD iteration (KSVD_FLAG_GRAPH): captured on a side stream, replayed.
+  // One cache for ksvd_iterate, one for ksvd_batched_iterate; a key lists every pointer and size
+  // the captured launches bake in.
+  struct GraphCache {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<const void*> key;
   };
   cudaStream_t gstream = nullptr;
   cudaEvent_t gev[2] = {nullptr, nullptr};
-  cudaGraphExec_t gexec = nullptr;
-  GraphKey gkey{};
+  GraphCache graphs[2];
   bool graph_broken = false;
   int64_t graph_replays = 0;
   // batched K-SVD: one child handle (own stream and workspace) per problem
@@ -587,7 +585,8 @@ void ksvd_destroy(ksvd_handle* h) {
   }
   for (auto e : h->kid_events) cudaEventDestroy(e);
   if (h->fork_ev) cudaEventDestroy(h->fork_ev);
-  if (h->gexec) cudaGraphExecDestroy(h->gexec);
+  for (auto& g : h->graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
   if (h->gstream) {
     cudaStreamSynchronize(h->gstream);
     cudaStreamDestroy(h->gstream);
@@ -733,9 +732,28 @@ ksvd_status ksvd_omp(ksvd_handle* h, const float* D, const float* X, int64_t N, 
 // Many independent problems: one grouped GEMM launch for every G_p = D_p'D_p and alpha0_p =
 // D_p'X_p, then one persistent Batch-OMP launch whose warps pull signal chunks of all problems
 // from a device work queue.
-ksvd_status ksvd_batched_omp(ksvd_handle* h, const ksvd_problem* probs, int32_t nprob) {
-  if (!h || nprob < 0 || (nprob > 0 && !probs)) return KSVD_ERR_INVALID_ARGUMENT;
-  if (nprob == 0) return KSVD_OK;
+namespace {
+
+// The device tables of one batched Batch-OMP call: the grouped GEMM's tile table (G_i = D_i'D_i
+// and alpha0_i = D_i'X_i) and the work queue's job table.
+struct BatchPlan {
+  GemmDesc* ddev = nullptr;
+  int nd = 0;
+  int64_t tiles = 0;
+  OmpJob* jdev = nullptr;
+  int nj = 0;
+  int64_t chunks = 0;
+  int tmax = 1;
+  int chunk = 1;
+  unsigned long long* queue = nullptr;
+  int* de = nullptr;
+};
+
+// Checks the problems, sizes the shared workspace and uploads the tables (asynchronously, from
+// host copies kept in the handle).  The tables depend only on the problems' sizes and pointers,
+// so a batched K-SVD call uploads them once and launches them every iteration.
+ksvd_status batched_omp_plan(ksvd_handle* h, const ksvd_problem* probs, int32_t nprob,
+                             BatchPlan* pl) {
   int64_t g_off = 0, a_off = 0;
   int tmax = 1;
   std::vector<int64_t> goff(nprob), aoff(nprob);
@@ -789,19 +807,37 @@ ksvd_status ksvd_batched_omp(ksvd_handle* h, const ksvd_problem* probs, int32_t 
     j.n = q.n; j.K = q.K; j.kpl = kp / 32; j.T = q.T;
     chunks += (q.N + chunk - 1) / chunk;
   }
+  *pl = BatchPlan{ddev, nd, tiles, jdev, nj, chunks, tmax, chunk, queue, de};
   if (nj == 0) return KSVD_OK;
   // the host tables live in the handle, so the asynchronous copies read valid memory
   KSVD_CK(h, cudaMemcpyAsync(ddev, descs.data(), sizeof(GemmDesc) * nd, cudaMemcpyHostToDevice,
                              h->stream));
   KSVD_CK(h, cudaMemcpyAsync(jdev, jobs.data(), sizeof(OmpJob) * nj, cudaMemcpyHostToDevice,
                              h->stream));
+  return KSVD_OK;
+}
+
+// The grouped GEMM and the persistent Batch-OMP launch of an uploaded plan.
+ksvd_status batched_omp_launch(ksvd_handle* h, const BatchPlan& pl) {
+  if (pl.nj == 0) return KSVD_OK;
   {
     StageScope sc(h, KSVD_STAGE_DTX);
-    KSVD_CK(h, launch_gemm_tn_f32_grouped(ddev, nd, tiles, h->stream));
+    KSVD_CK(h, launch_gemm_tn_f32_grouped(pl.ddev, pl.nd, pl.tiles, h->stream));
   }
   StageScope sc(h, KSVD_STAGE_OMP);
-  KSVD_CK(h, launch_omp_batched(jdev, nj, chunks, tmax, chunk, queue, de, h->stream));
+  KSVD_CK(h, launch_omp_batched(pl.jdev, pl.nj, pl.chunks, pl.tmax, pl.chunk, pl.queue, pl.de,
+                                h->stream));
   return KSVD_OK;
+}
+
+}  // namespace
+
+ksvd_status ksvd_batched_omp(ksvd_handle* h, const ksvd_problem* probs, int32_t nprob) {
+  if (!h || nprob < 0 || (nprob > 0 && !probs)) return KSVD_ERR_INVALID_ARGUMENT;
+  if (nprob == 0) return KSVD_OK;
+  BatchPlan pl;
+  KSVD_TRY(batched_omp_plan(h, probs, nprob, &pl));
+  return batched_omp_launch(h, pl);
 }
 
 namespace {
@@ -857,85 +893,6 @@ ksvd_status kid_error(ksvd_handle* h, ksvd_handle* k, ksvd_status s) {
 }
 
 }  // namespace
-
-// K-SVD on many independent problems.  Per iteration: ONE persistent Batch-OMP launch over all
-// problems (ksvd_batched_omp), then every problem's dictionary update, error and clearDict on
-// its own stream, concurrently; the cooperative sweeps share the SMs in proportion to each
-// problem's work (N*T), one CTA per SM in total, so they all fit on the GPU at once.
-ksvd_status ksvd_batched_iterate(ksvd_handle* h, ksvd_problem* probs, int32_t nprob,
-                                 int32_t iters, double* rmse) {
-  if (!h || nprob < 0 || (nprob > 0 && !probs) || iters < 0) return KSVD_ERR_INVALID_ARGUMENT;
-  if (nprob == 0 || iters == 0) return KSVD_OK;
-  if (iters > 1024) return fail(h, KSVD_ERR_UNSUPPORTED, "at most 1024 iterations per call%s");
-  for (int32_t i = 0; i < nprob; ++i)
-    if (probs[i].N < 1)
-      return fail(h, KSVD_ERR_INVALID_ARGUMENT, "every batched K-SVD problem needs N >= 1%s");
-  // workspace of the children first: the sweep CTA shares, dictionaries, permutations
-  int sms = 0;
-  KSVD_CK(h, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
-  double work = 0;
-  for (int32_t i = 0; i < nprob; ++i) work += (double)probs[i].N * probs[i].T;
-  std::vector<ksvd_handle*> ks(nprob);
-  std::vector<float*> Dp(nprob);
-  std::vector<int32_t*> pd(nprob);
-  std::vector<double*> rd(nprob);
-  std::vector<int32_t*> cd(nprob);
-  std::vector<ksvd_problem> inner(probs, probs + nprob);
-  const bool conc = h->batch_concurrent != 0;
-  int budget = sms - nprob;   // every problem has one CTA; the rest go by work
-  for (int32_t i = 0; i < nprob; ++i) {
-    KSVD_TRY(batch_child(h, i, probs[i], &ks[i]));
-    ksvd_handle* k = ks[i];
-    const int extra = budget > 0 ? (int)((double)budget * probs[i].N * probs[i].T / work) : 0;
-    // concurrent: shares that fit on the GPU together; sequential: every sweep gets all SMs
-    k->sweep_ctas = conc ? std::max(1, 1 + extra) : 0;
-  }
-  KSVD_TRY(batch_fork(h, nprob));
-  for (int32_t i = 0; i < nprob; ++i) {
-    ksvd_handle* k = ks[i];
-    if (bad_ptr(probs[i].D) || bad_ptr(probs[i].X))
-      return fail(h, KSVD_ERR_INVALID_ARGUMENT, "batched problem with a null pointer%s");
-    KSVD_TRY(kid_error(h, k, load_dict(k, probs[i].D, &Dp[i])));
-    KSVD_TRY(kid_error(h, k, ensure(k, B_RMSE, 1024, &rd[i])));
-    KSVD_TRY(kid_error(h, k, ensure(k, B_CLEARED, 1, &cd[i])));
-    KSVD_TRY(kid_error(h, k, upload_perm(k, nullptr, iters, &pd[i])));
-    KSVD_CK(h, launch_normcols(Dp[i], k->p.n, k->p.K, k->stream));   // KSVD.cu:57
-    inner[i].D = Dp[i];             // OMP codes with the children's working dictionaries
-  }
-  KSVD_TRY(batch_join(h, nprob));
-  for (int32_t it = 0; it < iters; ++it) {
-    KSVD_TRY(ksvd_batched_omp(h, inner.data(), nprob));
-    if (conc) KSVD_TRY(batch_fork(h, nprob));
-    for (int32_t i = 0; i < nprob; ++i) {
-      ksvd_handle* k = ks[i];
-      const ksvd_problem& q = probs[i];
-      // sequential mode runs every problem's stages on the parent stream, in order
-      const cudaStream_t own = k->stream;
-      if (!conc) k->stream = h->stream;
-      float* G = nullptr;
-      ksvd_status s2 = ensure(k, B_G, (size_t)k->Kp * k->Kp, &G);
-      if (s2 == KSVD_OK)
-        s2 = run_update(k, Dp[i], q.X, q.N, q.idx, q.coef, q.nnz, pd[i] + (size_t)it * q.K);
-      if (s2 == KSVD_OK) s2 = run_error(k, Dp[i], q.X, q.N, q.idx, q.coef, q.nnz, rd[i] + it);
-      if (s2 == KSVD_OK) s2 = gram_padded(k, Dp[i], G);
-      if (s2 == KSVD_OK) s2 = run_clear(k, Dp[i], G, q.X, q.N, cd[i]);
-      k->stream = own;
-      KSVD_TRY(kid_error(h, k, s2));
-    }
-    if (conc) KSVD_TRY(batch_join(h, nprob));
-  }
-  KSVD_TRY(batch_fork(h, nprob));
-  for (int32_t i = 0; i < nprob; ++i) {
-    KSVD_TRY(kid_error(h, ks[i], store_dict(ks[i], Dp[i], probs[i].D)));
-    if (rmse)
-      KSVD_CK(h, cudaMemcpyAsync(rmse + (size_t)i * iters, rd[i], sizeof(double) * iters,
-                                 cudaMemcpyDeviceToHost, ks[i]->stream));
-  }
-  KSVD_TRY(batch_join(h, nprob));
-  KSVD_CK(h, cudaStreamSynchronize(h->stream));
-  for (int32_t i = 0; i < nprob; ++i) KSVD_TRY(kid_error(h, ks[i], check_dev_err(ks[i])));
-  return check_dev_err(h);
-}
 
 }  // extern "C"
 
@@ -1290,23 +1247,24 @@ struct SideStream {
   }
 };
 
-// Replays `count` iterations from a graph of iteration_body, capturing it first when the cached
-// graph was made for other buffers.  Returns false (nothing launched) when capture is refused.
-bool replay_graph(ksvd_handle* h, const ksvd_handle::GraphKey& key, int32_t count, float* Dp,
-                  float* G, float* A0, const float* X, int64_t N, int32_t* idx, float* coef,
-                  int32_t* nnz, const int32_t* pd, double* rd, int32_t* cd, int* ctr) {
+// Replays `count` iterations from the graph in `cache`, capturing `body` (one iteration) first
+// when the cached graph was made for another key.  Returns false (nothing launched) when
+// capture is refused; the caller then runs the iterations eagerly.
+bool replay_graph(ksvd_handle* h, ksvd_handle::GraphCache& cache,
+                  const std::vector<const void*>& key, int32_t count,
+                  const std::function<ksvd_status()>& body) {
   if (h->graph_broken) return false;
-  if (!h->gexec || !(h->gkey == key)) {
-    if (h->gexec) {
-      cudaGraphExecDestroy(h->gexec);
-      h->gexec = nullptr;
+  if (!cache.exec || cache.key != key) {
+    if (cache.exec) {
+      cudaGraphExecDestroy(cache.exec);
+      cache.exec = nullptr;
     }
     if (cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
       cudaGetLastError();
       h->graph_broken = true;
       return false;
     }
-    const ksvd_status st = iteration_body(h, Dp, G, A0, X, N, idx, coef, nnz, pd, rd, cd, ctr);
+    const ksvd_status st = body();
     cudaGraph_t g = nullptr;
     const cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
     cudaGraphExec_t ex = nullptr;
@@ -1320,11 +1278,11 @@ bool replay_graph(ksvd_handle* h, const ksvd_handle::GraphKey& key, int32_t coun
       h->err.clear();
       return false;
     }
-    h->gexec = ex;
-    h->gkey = key;
+    cache.exec = ex;
+    cache.key = key;
   }
   for (int32_t r = 0; r < count; ++r)
-    if (cudaGraphLaunch(h->gexec, h->stream) != cudaSuccess) {
+    if (cudaGraphLaunch(cache.exec, h->stream) != cudaSuccess) {
       cudaGetLastError();
       return false;
     }
@@ -1405,11 +1363,13 @@ ksvd_status iterate_impl(ksvd_handle* h, float* D, const float* X, int64_t N, in
     done = 1;
   }
   if (graph && done < iters) {
-    ksvd_handle::GraphKey key{{Dp, G, A0, X, idx, coef, nnz, pd, rd, cd, ctr,
-                               reinterpret_cast<const void*>((intptr_t)h->p.precision),
-                               h->it_eps2},
-                              N};
-    if (replay_graph(h, key, iters - done, Dp, G, A0, X, N, idx, coef, nnz, pd, rd, cd, ctr))
+    const std::vector<const void*> key{
+        Dp, G, A0, X, idx, coef, nnz, pd, rd, cd, ctr,
+        reinterpret_cast<const void*>((intptr_t)h->p.precision), h->it_eps2,
+        reinterpret_cast<const void*>((intptr_t)N)};
+    if (replay_graph(h, h->graphs[0], key, iters - done, [&] {
+          return iteration_body(h, Dp, G, A0, X, N, idx, coef, nnz, pd, rd, cd, ctr);
+        }))
       done = iters;
   }
   for (; done < iters; ++done)
@@ -1430,6 +1390,118 @@ ksvd_status iterate_impl(ksvd_handle* h, float* D, const float* X, int64_t N, in
   return check_dev_err(h);
 }
 }  // namespace
+
+// K-SVD on many independent problems.  Per iteration: ONE persistent Batch-OMP launch over all
+// problems (the batched plan's tables are uploaded once per call), then every problem's
+// dictionary update, error and clearDict -- one after another on the parent stream, each sweep
+// on the whole GPU (sequential mode), or on the problems' own streams at once with the SMs
+// shared in proportion to each problem's work N*T (concurrent mode).  Every problem has a
+// device iteration counter that selects its permutation and RMSE slot, so with KSVD_FLAG_GRAPH
+// the second and later iterations replay one captured graph of the whole batched iteration.
+ksvd_status ksvd_batched_iterate(ksvd_handle* h, ksvd_problem* probs, int32_t nprob,
+                                 int32_t iters, double* rmse) {
+  if (!h || nprob < 0 || (nprob > 0 && !probs) || iters < 0) return KSVD_ERR_INVALID_ARGUMENT;
+  if (nprob == 0 || iters == 0) return KSVD_OK;
+  if (iters > 1024) return fail(h, KSVD_ERR_UNSUPPORTED, "at most 1024 iterations per call%s");
+  for (int32_t i = 0; i < nprob; ++i)
+    if (probs[i].N < 1)
+      return fail(h, KSVD_ERR_INVALID_ARGUMENT, "every batched K-SVD problem needs N >= 1%s");
+  const bool graph = (h->p.flags & KSVD_FLAG_GRAPH) && !h->profiling() && iters > 1;
+  SideStream side(h);
+  if (graph) KSVD_TRY(side.enter());
+  // workspace of the children first: the sweep CTA shares, dictionaries, permutations
+  int sms = 0;
+  KSVD_CK(h, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
+  double work = 0;
+  for (int32_t i = 0; i < nprob; ++i) work += (double)probs[i].N * probs[i].T;
+  std::vector<ksvd_handle*> ks(nprob);
+  std::vector<float*> Dp(nprob);
+  std::vector<int32_t*> pd(nprob);
+  std::vector<double*> rd(nprob);
+  std::vector<int32_t*> cd(nprob);
+  std::vector<int*> ctr(nprob);
+  std::vector<ksvd_problem> inner(probs, probs + nprob);
+  const bool conc = h->batch_concurrent != 0;
+  int budget = sms - nprob;   // every problem has one CTA; the rest go by work
+  for (int32_t i = 0; i < nprob; ++i) {
+    KSVD_TRY(batch_child(h, i, probs[i], &ks[i]));
+    ksvd_handle* k = ks[i];
+    const int extra = budget > 0 ? (int)((double)budget * probs[i].N * probs[i].T / work) : 0;
+    // concurrent: shares that fit on the GPU together; sequential: every sweep gets all SMs
+    k->sweep_ctas = conc ? std::max(1, 1 + extra) : 0;
+  }
+  KSVD_TRY(batch_fork(h, nprob));
+  for (int32_t i = 0; i < nprob; ++i) {
+    ksvd_handle* k = ks[i];
+    if (bad_ptr(probs[i].D) || bad_ptr(probs[i].X))
+      return fail(h, KSVD_ERR_INVALID_ARGUMENT, "batched problem with a null pointer%s");
+    KSVD_TRY(kid_error(h, k, load_dict(k, probs[i].D, &Dp[i])));
+    KSVD_TRY(kid_error(h, k, ensure(k, B_RMSE, 1024, &rd[i])));
+    KSVD_TRY(kid_error(h, k, ensure(k, B_CLEARED, 1, &cd[i])));
+    KSVD_TRY(kid_error(h, k, ensure(k, B_ITER, 1, &ctr[i])));
+    KSVD_TRY(kid_error(h, k, upload_perm(k, nullptr, iters, &pd[i])));
+    KSVD_CK(h, cudaMemsetAsync(ctr[i], 0, sizeof(int), k->stream));
+    KSVD_CK(h, launch_normcols(Dp[i], k->p.n, k->p.K, k->stream));   // KSVD.cu:57
+    inner[i].D = Dp[i];             // OMP codes with the children's working dictionaries
+  }
+  KSVD_TRY(batch_join(h, nprob));
+  BatchPlan plan;
+  KSVD_TRY(batched_omp_plan(h, inner.data(), nprob, &plan));
+  auto one_iteration = [&]() -> ksvd_status {
+    KSVD_TRY(batched_omp_launch(h, plan));
+    if (conc) KSVD_TRY(batch_fork(h, nprob));
+    for (int32_t i = 0; i < nprob; ++i) {
+      ksvd_handle* k = ks[i];
+      const ksvd_problem& q = probs[i];
+      // sequential mode runs every problem's stages on the parent stream, in order
+      const cudaStream_t own = k->stream;
+      if (!conc) k->stream = h->stream;
+      float* G = nullptr;
+      ksvd_status s2 = ensure(k, B_G, (size_t)k->Kp * k->Kp, &G);
+      if (s2 == KSVD_OK)
+        s2 = run_update(k, Dp[i], q.X, q.N, q.idx, q.coef, q.nnz, pd[i], ctr[i]);
+      if (s2 == KSVD_OK) s2 = run_error(k, Dp[i], q.X, q.N, q.idx, q.coef, q.nnz, rd[i], ctr[i]);
+      if (s2 == KSVD_OK) s2 = gram_padded(k, Dp[i], G);
+      if (s2 == KSVD_OK) s2 = run_clear(k, Dp[i], G, q.X, q.N, cd[i]);
+      if (s2 == KSVD_OK) {
+        const cudaError_t e = launch_advance_counter(ctr[i], k->stream);
+        if (e != cudaSuccess) s2 = cuda_fail(k, e, "launch_advance_counter");
+      }
+      k->stream = own;
+      KSVD_TRY(kid_error(h, k, s2));
+    }
+    if (conc) KSVD_TRY(batch_join(h, nprob));
+    return KSVD_OK;
+  };
+  // the first iteration runs eagerly: it sizes every child's workspace (nothing may be
+  // allocated under capture)
+  KSVD_TRY(one_iteration());
+  int32_t done = 1;
+  if (graph && done < iters) {
+    std::vector<const void*> key{reinterpret_cast<const void*>((intptr_t)conc),
+                                 plan.ddev, plan.jdev,
+                                 reinterpret_cast<const void*>((intptr_t)plan.chunk)};
+    for (int32_t i = 0; i < nprob; ++i) {
+      const ksvd_problem& q = probs[i];
+      key.insert(key.end(), {ks[i], Dp[i], q.X, q.idx, q.coef, q.nnz, pd[i], rd[i], cd[i],
+                             ctr[i], reinterpret_cast<const void*>((intptr_t)q.N),
+                             reinterpret_cast<const void*>((intptr_t)ks[i]->sweep_ctas)});
+    }
+    if (replay_graph(h, h->graphs[1], key, iters - done, one_iteration)) done = iters;
+  }
+  for (; done < iters; ++done) KSVD_TRY(one_iteration());
+  KSVD_TRY(batch_fork(h, nprob));
+  for (int32_t i = 0; i < nprob; ++i) {
+    KSVD_TRY(kid_error(h, ks[i], store_dict(ks[i], Dp[i], probs[i].D)));
+    if (rmse)
+      KSVD_CK(h, cudaMemcpyAsync(rmse + (size_t)i * iters, rd[i], sizeof(double) * iters,
+                                 cudaMemcpyDeviceToHost, ks[i]->stream));
+  }
+  KSVD_TRY(batch_join(h, nprob));
+  KSVD_CK(h, cudaStreamSynchronize(h->stream));
+  for (int32_t i = 0; i < nprob; ++i) KSVD_TRY(kid_error(h, ks[i], check_dev_err(ks[i])));
+  return check_dev_err(h);
+}
 
 ksvd_status ksvd_iterate_host(ksvd_handle* h, float* D, const float* X, int64_t N, int32_t iters,
                               const int32_t* perms, int32_t* idx, float* coef, int32_t* nnz,

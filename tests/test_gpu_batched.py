@@ -138,6 +138,45 @@ def test_batched_iterate_matches_single_problem_runs(cuda, concurrent):
     hb.close()
 
 
+@pytest.mark.parametrize("concurrent", [0, 1])
+def test_batched_iterate_graph_replay_matches_plain_launches(cuda, concurrent):
+    """KSVD_FLAG_GRAPH on the parent handle: the batched iterations 2..iters replay one captured
+    CUDA graph of the whole batched iteration (batched OMP, then every problem's update, error
+    and clearDict), with each problem's permutation and RMSE slot picked by its device iteration
+    counter.  Per-iteration RMSE equals the plain-launch run's (up to the atomics' summation
+    order), the dictionaries agree, and a second call on the same buffers replays the cached
+    graph."""
+    import torch
+
+    from ksvd_gb300 import Handle
+
+    probs = make_problems(11, [(32, 3000), (64, 2500), (128, 3000)])
+    res = []
+    for graph in (False, True):
+        dev = [dict(D=torch.from_numpy(np.ascontiguousarray(q["D"].T)).to(cuda),
+                    X=torch.from_numpy(np.ascontiguousarray(q["X"].T)).to(cuda), T=6)
+               for q in probs]
+        hb = Handle(1, 1, 1, seed=7, graph=graph)
+        hb.tuning = dict(hb.tuning, batch_concurrent=concurrent)
+        outs, rmse = hb.batched_iterate(dev, 3)
+        hb.synchronize()
+        res.append(([d["D"].clone() for d in dev], rmse, hb.graph_replays()))
+        if graph:
+            for d, q in zip(dev, probs):
+                d["D"].copy_(torch.from_numpy(np.ascontiguousarray(q["D"].T)).to(cuda))
+            outs, rmse_again = hb.batched_iterate(dev, 3, out=outs)
+            hb.synchronize()
+            assert hb.graph_replays() == 4                # the cached graph was replayed again
+            assert np.all(np.isfinite(rmse_again)) and np.all(rmse_again > 0)
+        hb.close()
+    (Da, ra, ga), (Db, rb, gb) = res
+    assert ga == 0 and gb == 2
+    np.testing.assert_allclose(rb, ra, rtol=1e-4)
+    for a, b in zip(Da, Db):
+        col = np.linalg.norm(a.double().cpu().numpy() - b.double().cpu().numpy(), axis=1)
+        assert np.mean(col <= 1e-3) >= 0.99, np.sort(col)[-10:]
+
+
 def test_batched_autotune_restores_dictionaries(cuda):
     import torch
 
