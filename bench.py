@@ -132,7 +132,11 @@ def stage_flops(cfg, N, stage):
 # DRAM bytes per signal of one launch, from ncu captures (dram__bytes_read.sum +
 # dram__bytes_write.sum) of the same kernel on 100,000 signals of the same (n, K, T); traffic grows
 # in proportion to the signals, so the bench scales it to its N.  profiles/omp_kernel_cfg2.md.
-MEASURED_TRAFFIC = {("omp", 256, 1024, 16): (414.642432e6 + 7.440128e6) / 100_000}
+MEASURED_TRAFFIC = {("omp", 256, 1024, 16): (414.144256e6 + 7.270400e6) / 100_000}
+
+# The unit that binds Batch-OMP is L2 (G's support columns re-read every step): L2 throughput in
+# percent of peak (lts__throughput.avg.pct_of_peak_sustained_elapsed) from the same capture.
+MEASURED_L2_PCT = {("omp", 256, 1024, 16): 69.75}
 
 # FP32 CUDA-core peak (nominal): 152 SMs x 128 FMA lanes x 2 FLOP x 2.07 GHz.
 FP32_SIMT_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
@@ -605,6 +609,11 @@ def main():
         tf = fl / (launch_ms / 1e3) / 1e12
         roof["compute"] = {"achieved": tf, "peak": FP32_SIMT_TFLOPS, "unit": "TFLOP/s",
                            "frac": tf / FP32_SIMT_TFLOPS, "peak_source": "nominal FP32 SIMT"}
+        l2 = MEASURED_L2_PCT.get((dom, cfg.n, cfg.K, cfg.T))
+        if l2 is not None:
+            roof["l2"] = {"throughput_pct_of_peak": l2,
+                          "source": "ncu lts__throughput at N=100000 (profiles/omp_kernel_cfg2.md)",
+                          "support_column_bytes": float(N) * cfg.K * 4 * cfg.T * (cfg.T - 1) / 2}
     roof["kernel"] = dom
     roof["peak_source"] = pk["src"]
     stage_summary = {k: {"ms_per_launch": round(v[0], 4), "share": round(v[0] * v[1] / sum(
