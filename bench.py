@@ -35,9 +35,10 @@ if ROOT not in sys.path:
 # dictionary splits)
 # library kernels per ksvd_iterate call: copy_pad_cols, normcols, Gram (mixed: + BF16 splits of D
 # and X); per iteration: D'X, OMP, Gram, 4 list kernels, init_state, prepare, P = D'Y, sweep,
-# error + rmse, Gram, coherence + clear_seq, advance_counter (mixed: + 3 BF16 splits of D)
+# error + rmse, Gram, coherence + clear_seq, advance_counter (mixed: + 3 BF16 splits of D and
+# the FP16 copy of G for Batch-OMP)
 KERNELS_PER_CALL = {"fp32": 3, "mixed": 5}
-KERNELS_PER_ITER = {"fp32": 17, "mixed": 20}
+KERNELS_PER_ITER = {"fp32": 17, "mixed": 21}
 
 
 def peaks():

@@ -100,7 +100,7 @@ enum BufId {
   B_DPAD, B_G, B_A0, B_XN2, B_LIST, B_START, B_BHIST, B_Y, B_GN2, B_C, B_AVEC, B_AD, B_PART,
   B_UNUSED, B_BITMAP, B_REPLACED, B_COUNTER, B_USE, B_BARRIER, B_ERR, B_PSUM, B_BVAL, B_BIDX,
   B_RMSE, B_M, B_MI, B_CLEARED, B_DEVERR, B_PERM, B_GPAD_IN, B_HX, B_HD, B_HIDX, B_HCOEF, B_HNNZ,
-  B_XHI, B_XLO, B_DHI, B_DLO, B_P, B_BG, B_BA0, B_BDESC, B_BJOB, B_BQUEUE, B_ITER, B_RPART, B_RMEAN, B_TUNE_D, B_TUNE_C, B_COUNT
+  B_XHI, B_XLO, B_DHI, B_DLO, B_P, B_BG, B_BA0, B_BDESC, B_BJOB, B_BQUEUE, B_ITER, B_RPART, B_RMEAN, B_TUNE_D, B_TUNE_C, B_GH, B_MU, B_COUNT
 };
 
 ksvd_status fail(ksvd_handle* h, ksvd_status s, const char* fmt, const char* detail = nullptr) {
@@ -340,9 +340,18 @@ ksvd_status run_omp(ksvd_handle* h, const float* G, const float* A0, int64_t N,
                     int32_t* nnz) {
   int* de = nullptr;
   KSVD_TRY(ensure(h, B_DEVERR, 1, &de));
+  // mixed path: the alpha update reads an FP16 copy of G (made here, G may have changed since
+  // the last call) and resolves near ties in FP32
+  uint16_t* gh = nullptr;
+  unsigned* mu = nullptr;
+  if (mixed(h) && h->p.T <= 32) {
+    KSVD_TRY(ensure(h, B_GH, (size_t)h->Kp * h->Kp, &gh));
+    KSVD_TRY(ensure(h, B_MU, 1, &mu));
+  }
   StageScope sc(h, KSVD_STAGE_OMP);
+  if (gh) KSVD_CK(h, launch_gram_half(G, h->Kp, h->p.K, gh, mu, h->stream));
   KSVD_CK(h, launch_omp(G, h->Kp, A0, h->Kp, h->p.K, N, h->p.T, xnorm2, eps2, idx, coef, nnz, de,
-                        h->stream, h->omp_grid_mult));
+                        h->stream, h->omp_grid_mult, gh, mu));
   return KSVD_OK;
 }
 

@@ -39,10 +39,16 @@ int omp_padded_k(int K);
 // G: Kp x Kp column-major (ldg >= Kp), zero padded; A0: Kp x N column-major (lda >= Kp), zero
 // padded, with Kp = omp_padded_k(K).  T <= 64.
 // grid_mult: resident CTAs per SM x grid_mult blocks at most (0 = default 8; the autotuner's knob)
+// Gh/mu (mixed path, T <= 32): FP16 copy of G and its coherence from launch_gram_half; the alpha
+// update then reads Gh and resolves near ties in FP32 (the selection is the FP32 Batch-OMP's).
 cudaError_t launch_omp(const float* G, int64_t ldg, const float* A0, int64_t lda, int K,
                        int64_t N, int T, const float* xnorm2, const float* eps2, int32_t* idx,
                        float* coef, int32_t* nnz, int* dev_err, cudaStream_t st,
-                       int grid_mult = 0);
+                       int grid_mult = 0, const uint16_t* Gh = nullptr,
+                       const unsigned* mu = nullptr);
+// Gh = FP16(G) (Kp x Kp, same ldg) and mu = max off-diagonal |G(i, j)|, i, j < K.
+cudaError_t launch_gram_half(const float* G, int64_t ldg, int K, uint16_t* Gh, unsigned* mu,
+                             cudaStream_t st);
 
 // ---- misc (misc.cu) ---------------------------------------------------------------------------
 cudaError_t launch_normcols(float* D, int n, int K, cudaStream_t st);

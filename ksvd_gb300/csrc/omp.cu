@@ -14,6 +14,10 @@
 // last atom is skipped (it is never read), and a failed pivot test does not add the atom.
 // alpha0 is streamed once (evict-first loads); G stays L2-resident, and re-reading the support
 // columns of G from L2 (N*K*T(T-1)/2 floats per sweep of all signals) is what bounds this kernel.
+#include <cuda_fp16.h>
+
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -60,56 +64,232 @@ __device__ __forceinline__ void put(V (&a)[SPL], int j, V v) {
   else { if (j == 0) a[0] = v; else a[1] = v; }
 }
 
+// 8-byte read-only load (four FP16 values) that does not allocate in L1
+__device__ __forceinline__ uint2 ldg_u2_no_l1(const void* p) {
+  uint2 g;
+  asm volatile("ld.global.nc.L1::no_allocate.v2.u32 {%0,%1}, [%2];"
+               : "=r"(g.x), "=r"(g.y)
+               : "l"(p));
+  return g;
+}
+
+// 16-byte read-only load (eight FP16 values) that does not allocate in L1
+__device__ __forceinline__ uint4 ldg_u4_no_l1(const void* p) {
+  uint4 g;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(g.x), "=r"(g.y), "=r"(g.z), "=r"(g.w)
+               : "l"(p));
+  return g;
+}
+
+// a0 += lo(g) * c, a1 += hi(g) * c: FP16 products accumulated in FP32 (one mixed-precision FMA
+// per element, no conversion instructions)
+__device__ __forceinline__ void fma2_f16_f32(uint32_t g, unsigned short c, float& a0, float& a1) {
+  asm("{\n .reg .f16 lo, hi;\n mov.b32 {lo, hi}, %2;\n fma.rn.f32.f16 %0, lo, %3, %0;\n"
+      " fma.rn.f32.f16 %1, hi, %3, %1;\n}"
+      : "+f"(a0), "+f"(a1)
+      : "r"(g), "h"(c));
+}
+
+// Near-tie resolution of the FP16 alpha update: at most this many atoms are re-evaluated in FP32
+// per step; more candidates (or a maximum too small to trust) recompute the whole alpha in FP32.
+constexpr int kMaxCand = 8;
+
 // Batch-OMP of one signal by one warp.  a0p: the signal's alpha0 column (Kp = 32*KPL rows, rows
-// >= K zero); L: (TMAX x TMAX+1) and a0s: (32*KPL) floats of this warp's shared memory.  emode:
-// stop once ||x||^2 - ||y||^2 <= e2 (xn2 = ||x||^2).  Writes T slots of idx/coef and nnz.
-template <int KPL, int TMAX>
-__device__ __forceinline__ void omp_signal(const float* __restrict__ G, int64_t ldg,
-                                           const float* __restrict__ a0col, int K, int T,
-                                           bool emode, float e2, float xn2,
+// >= K zero); L: (TMAX x TMAX+1) and a0s: (32*KPL) floats, cand: kMaxCand ints of this warp's
+// shared memory.  emode: stop once ||x||^2 - ||y||^2 <= e2 (xn2 = ||x||^2).  Writes T slots of
+// idx/coef and nnz.
+//
+// H16 (mixed path): alpha = alpha0 - G(:, I) c is formed from an FP16 copy Gh of G (half the L2
+// bytes of the re-read support columns; c scaled by a power of two into FP16 range, products
+// accumulated in FP32).  Its error per atom is below 2^-10 sum_r |G(k, I_r) c_r|; the allowance
+// errb = tol * ||c||_1 (tol = 2^-12 mu + 2^-20, mu the dictionary's coherence) is a quarter of
+// that worst case and ~10x the rounding error's spread.  Every atom whose approximate |alpha|
+// lies within 2 errb of the maximum is re-evaluated in FP32 with exactly the FP32 path's
+// operations, so the selection, the stop tests and the coefficients are those of the FP32
+// Batch-OMP; with more than kMaxCand candidates, or a maximum below 4 errb, the step's alpha is
+// recomputed in FP32.
+template <int KPL, int TMAX, bool H16, bool CHECKK>
+__device__ __forceinline__ void omp_signal(const float* __restrict__ G,
+                                           const uint16_t* __restrict__ Gh, float tol,
+                                           int64_t ldg, const float* __restrict__ a0col, int K,
+                                           int T, bool emode, float e2, float xn2,
                                            int32_t* __restrict__ idx_s, float* __restrict__ coef_s,
                                            int32_t* __restrict__ nnz_s, float* L, float* a0s,
-                                           bool& numeric_bad) {
-  constexpr int M4 = KPL / 4;    // float4 groups per lane; lane owns rows 128*m + 4*lane + q
+                                           int* cand, bool& numeric_bad) {
+  // lane layout of alpha: groups of V consecutive rows, lane owns rows 32*V*g + V*lane + q
+  // (V = 8 lets the FP16 update read 16 bytes per load)
+  constexpr int V = (H16 && KPL >= 8) ? 8 : 4;
+  constexpr int NG = KPL / V;
   constexpr int SPL = TMAX / 32; // support slots per lane; lane owns slots lane + 32*j
+  static_assert(!H16 || TMAX == 32, "the FP16 update serves supports of up to 32 atoms");
   const int lane = threadIdx.x & 31;
+  // rows >= K of G and alpha0 are zero, so their alpha stays 0 (or NaN) and never wins a strict
+  // comparison against the first real atom; CHECKK keeps the explicit test for callers whose
+  // padding is not guaranteed
+  auto real = [&](int k) { return !CHECKK || k < K; };
   {
-    float al[M4][4];
-    const float* a0p = a0col + 4 * lane;
+    float al[NG][V];
+    const float* a0p = a0col + V * lane;
     __syncwarp();                      // the previous signal's last reads of a0s are done
 #pragma unroll
-    for (int m = 0; m < M4; ++m) {
-      const float4 v = __ldcs(reinterpret_cast<const float4*>(a0p + 128 * m));
-      *reinterpret_cast<float4*>(a0s + 128 * m + 4 * lane) = v;
-      al[m][0] = v.x; al[m][1] = v.y; al[m][2] = v.z; al[m][3] = v.w;
-    }
+    for (int g = 0; g < NG; ++g)
+#pragma unroll
+      for (int h = 0; h < V / 4; ++h) {
+        const float4 v = __ldcs(reinterpret_cast<const float4*>(a0p + 32 * V * g + 4 * h));
+        *reinterpret_cast<float4*>(a0s + 32 * V * g + V * lane + 4 * h) = v;
+        al[g][4 * h] = v.x; al[g][4 * h + 1] = v.y; al[g][4 * h + 2] = v.z; al[g][4 * h + 3] = v.w;
+      }
     __syncwarp();
     int ind[SPL];
     float y[SPL], c[SPL];
 #pragma unroll
     for (int j = 0; j < SPL; ++j) { ind[j] = -1; y[j] = 0.f; c[j] = 0.f; }
 
-    float r2 = xn2;
-    int i = 0;
-    while (i < T) {
-      if (emode && r2 <= e2) break;
-      // ---- argmax |alpha| (first maximum) with alpha_p as payload
-      float bv = -1.f, bal = 0.f;
-      int bk = 0x7fffffff;
+    // alpha = alpha0 - G(:, I) c in FP32: one support column per step, in slot order (deeper
+    // unrolling measured slower: register pressure); G's columns bypass L1 allocation -- they
+    // are reused from L2, not from L1
+    auto exact_alpha = [&](int i) {
 #pragma unroll
-      for (int m = 0; m < M4; ++m)
+      for (int g = 0; g < NG; ++g)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int k = 128 * m + 4 * lane + q;
-          const float v = al[m][q] * al[m][q];
-          if (k < K && v > bv) { bv = v; bk = k; bal = al[m][q]; }
+        for (int q = 0; q < V; ++q) al[g][q] = 0.f;
+#pragma unroll 1
+      for (int r = 0; r < i; ++r) {
+        const int rl = r & 31, rj = r >> 5;
+        const float cr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(c, rj), rl);
+        const int col = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(ind, rj), rl);
+        const float* gp = G + (int64_t)col * ldg + V * lane;
+#pragma unroll
+        for (int g = 0; g < NG; ++g)
+#pragma unroll
+          for (int h = 0; h < V / 4; ++h) {
+            const float4 gv = ldg_f4_no_l1(gp + 32 * V * g + 4 * h);
+            al[g][4 * h] = fmaf(gv.x, cr, al[g][4 * h]);
+            al[g][4 * h + 1] = fmaf(gv.y, cr, al[g][4 * h + 1]);
+            al[g][4 * h + 2] = fmaf(gv.z, cr, al[g][4 * h + 2]);
+            al[g][4 * h + 3] = fmaf(gv.w, cr, al[g][4 * h + 3]);
+          }
+      }
+#pragma unroll
+      for (int g = 0; g < NG; ++g)
+#pragma unroll
+        for (int h = 0; h < V / 4; ++h) {
+          const float4 a =
+              *reinterpret_cast<const float4*>(a0s + 32 * V * g + V * lane + 4 * h);
+          al[g][4 * h] = a.x - al[g][4 * h];
+          al[g][4 * h + 1] = a.y - al[g][4 * h + 1];
+          al[g][4 * h + 2] = a.z - al[g][4 * h + 2];
+          al[g][4 * h + 3] = a.w - al[g][4 * h + 3];
+        }
+    };
+    // argmax of alpha^2 (first maximum); alpha_p^2 is the stop test's value
+    auto argmax = [&](float& bv, int& bk) {
+      bv = -1.f; bk = 0x7fffffff;
+#pragma unroll
+      for (int g = 0; g < NG; ++g)
+#pragma unroll
+        for (int q = 0; q < V; ++q) {
+          const int k = 32 * V * g + V * lane + q;
+          const float v = al[g][q] * al[g][q];
+          if (real(k) && v > bv) { bv = v; bk = k; }
         }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         const float ov = __shfl_xor_sync(KSVD_FULL_MASK, bv, o);
         const int ok = __shfl_xor_sync(KSVD_FULL_MASK, bk, o);
-        const float oal = __shfl_xor_sync(KSVD_FULL_MASK, bal, o);
-        if (ov > bv || (ov == bv && ok < bk)) { bv = ov; bk = ok; bal = oal; }
+        if (ov > bv || (ov == bv && ok < bk)) { bv = ov; bk = ok; }
+      }
+    };
+
+    float r2 = xn2;
+    int i = 0;
+    bool approx = false;   // al holds the FP16 update's alpha
+    float errb = 0.f;      // its error allowance per atom
+    // this lane's two largest approximate |alpha| (with the first maximum's atom), formed by the
+    // FP16 update's last pass
+    float hv1 = -1.f, hv2 = -1.f;
+    int hk = 0x7fffffff;
+    while (i < T) {
+      if (emode && r2 <= e2) break;
+      float bv;
+      int bk;
+      if (!H16 || !approx) argmax(bv, bk);
+      if constexpr (H16) {
+        if (approx) {
+          approx = false;
+          // warp maximum and runner-up of the approximate |alpha|
+          float b2 = hv2, b1 = hv1;
+          bk = hk;
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            const float ov = __shfl_xor_sync(KSVD_FULL_MASK, b1, o);
+            const int ok = __shfl_xor_sync(KSVD_FULL_MASK, bk, o);
+            const float o2 = __shfl_xor_sync(KSVD_FULL_MASK, b2, o);
+            if (ov > b1 || (ov == b1 && ok < bk)) {
+              b2 = fmaxf(b1, o2); b1 = ov; bk = ok;
+            } else {
+              b2 = fmaxf(b2, ov);
+            }
+          }
+          bv = b1 * b1;
+          const float thr = b1 - 2.f * errb;
+          bool full = !(b1 > 4.f * errb) || !(b1 > 1e-6f);
+          if (!full && !(b2 < thr)) {
+            // near tie: every atom within 2 errb of the maximum is a candidate
+            unsigned mine = 0;
+#pragma unroll
+            for (int g = 0; g < NG; ++g)
+#pragma unroll
+              for (int q = 0; q < V; ++q) {
+                const int k = 32 * V * g + V * lane + q;
+                if (real(k) && fabsf(al[g][q]) >= thr) mine |= 1u << (V * g + q);
+              }
+            const int cnt = __popc(mine);
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+              const int t = __shfl_up_sync(KSVD_FULL_MASK, incl, o);
+              if (lane >= o) incl += t;
+            }
+            const int total = __shfl_sync(KSVD_FULL_MASK, incl, 31);
+            full = total > kMaxCand;
+            if (!full) {
+              // the candidates' alpha in FP32, in the FP32 update's order of operations
+              int at = incl - cnt;
+              while (mine) {
+                const int b = __ffs(mine) - 1;
+                mine &= mine - 1;
+                cand[at++] = 32 * V * (b / V) + V * lane + (b % V);
+              }
+              __syncwarp();
+              const bool mine_c = lane < total;
+              const int kc = mine_c ? cand[lane] : 0;
+              float ale = 0.f;
+#pragma unroll 4
+              for (int r = 0; r < i; ++r) {
+                const int rl = r & 31, rj = r >> 5;
+                const float cr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(c, rj), rl);
+                const int col = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(ind, rj), rl);
+                if (mine_c) ale = fmaf(__ldg(G + (int64_t)col * ldg + kc), cr, ale);
+              }
+              const float ae = mine_c ? a0s[kc] - ale : 0.f;
+              bv = mine_c ? ae * ae : -1.f;
+              bk = mine_c ? kc : 0x7fffffff;
+#pragma unroll
+              for (int o = 16; o > 0; o >>= 1) {
+                const float ov = __shfl_xor_sync(KSVD_FULL_MASK, bv, o);
+                const int ok = __shfl_xor_sync(KSVD_FULL_MASK, bk, o);
+                if (ov > bv || (ov == bv && ok < bk)) { bv = ov; bk = ok; }
+              }
+              __syncwarp();                    // cand is read before the next step writes it
+            }
+          }
+          if (full) {
+            exact_alpha(i);
+            argmax(bv, bk);
+          }
+        }
       }
       if (bk >= K) { numeric_bad = true; break; }   // every |alpha| was NaN
       const int p = bk;
@@ -118,7 +298,7 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G, int64_t 
 #pragma unroll
       for (int j = 0; j < SPL; ++j) dup |= (lane + 32 * j < i) && ind[j] == p;
       if (__any_sync(KSVD_FULL_MASK, dup)) break;
-      if (bal * bal < 1e-14f) break;
+      if (bv < 1e-14f) break;                // alpha_p^2 (OMP.cu:304)
 
       float Lii = 1.f, ynew = ba0;
       if (i > 0) {
@@ -187,34 +367,69 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G, int64_t 
       }
       // ---- alpha = alpha0 - G(:, I) c   (not needed after the last atom)
       if (i < T && !(emode && r2 <= e2)) {
+        if constexpr (H16) {
+          float cmx = 0.f, cl1 = 0.f;
 #pragma unroll
-        for (int m = 0; m < M4; ++m)
+          for (int j = 0; j < SPL; ++j)
+            if (lane + 32 * j < i) { cmx = fmaxf(cmx, fabsf(c[j])); cl1 += fabsf(c[j]); }
+          cmx = warp_max(cmx);
+          cl1 = warp_sum(cl1);
+          int ex = 0;
+          frexpf(cmx, &ex);                    // |c| / 2^ex < 1: no FP16 overflow
+          const float csc = ldexpf(1.f, ex), cisc = ldexpf(1.f, -ex);
 #pragma unroll
-          for (int q = 0; q < 4; ++q) al[m][q] = 0.f;
-        // one support column per step (deeper unrolling measured slower: register pressure);
-        // G's columns bypass L1 allocation -- they are reused from L2, not from L1
+          for (int g = 0; g < NG; ++g)
+#pragma unroll
+            for (int q = 0; q < V; ++q) al[g][q] = 0.f;
 #pragma unroll 1
-        for (int r = 0; r < i; ++r) {
-          const int rl = r & 31, rj = r >> 5;
-          const float cr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(c, rj), rl);
-          const int col = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(ind, rj), rl);
-          const float* gp = G + (int64_t)col * ldg + 4 * lane;
+          for (int r = 0; r < i; ++r) {
+            const int rl = r & 31, rj = r >> 5;
+            const float cr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(c, rj), rl);
+            const int col = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(ind, rj), rl);
+            const unsigned short ch = __half_as_ushort(__float2half_rn(cr * cisc));
+            const uint16_t* gp = Gh + (int64_t)col * ldg + V * lane;
 #pragma unroll
-          for (int m = 0; m < M4; ++m) {
-            const float4 g = ldg_f4_no_l1(gp + 128 * m);
-            al[m][0] = fmaf(g.x, cr, al[m][0]);
-            al[m][1] = fmaf(g.y, cr, al[m][1]);
-            al[m][2] = fmaf(g.z, cr, al[m][2]);
-            al[m][3] = fmaf(g.w, cr, al[m][3]);
+            for (int g = 0; g < NG; ++g) {
+              if constexpr (V == 8) {
+                const uint4 gv = ldg_u4_no_l1(gp + 256 * g);
+                fma2_f16_f32(gv.x, ch, al[g][0], al[g][1]);
+                fma2_f16_f32(gv.y, ch, al[g][2], al[g][3]);
+                fma2_f16_f32(gv.z, ch, al[g][4], al[g][5]);
+                fma2_f16_f32(gv.w, ch, al[g][6], al[g][7]);
+              } else {
+                const uint2 gv = ldg_u2_no_l1(gp + 128 * g);
+                fma2_f16_f32(gv.x, ch, al[g][0], al[g][1]);
+                fma2_f16_f32(gv.y, ch, al[g][2], al[g][3]);
+              }
+            }
           }
-        }
+          hv1 = -1.f; hv2 = -1.f; hk = 0x7fffffff;
 #pragma unroll
-        for (int m = 0; m < M4; ++m) {
-          const float4 a = *reinterpret_cast<const float4*>(a0s + 128 * m + 4 * lane);
-          al[m][0] = a.x - al[m][0];
-          al[m][1] = a.y - al[m][1];
-          al[m][2] = a.z - al[m][2];
-          al[m][3] = a.w - al[m][3];
+          for (int g = 0; g < NG; ++g)
+#pragma unroll
+            for (int h = 0; h < V / 4; ++h) {
+              const float4 a =
+                  *reinterpret_cast<const float4*>(a0s + 32 * V * g + V * lane + 4 * h);
+              al[g][4 * h] = fmaf(-csc, al[g][4 * h], a.x);
+              al[g][4 * h + 1] = fmaf(-csc, al[g][4 * h + 1], a.y);
+              al[g][4 * h + 2] = fmaf(-csc, al[g][4 * h + 2], a.z);
+              al[g][4 * h + 3] = fmaf(-csc, al[g][4 * h + 3], a.w);
+            }
+#pragma unroll
+          for (int g = 0; g < NG; ++g)
+#pragma unroll
+            for (int q = 0; q < V; ++q) {
+              const int k = 32 * V * g + V * lane + q;
+              const float v = fabsf(al[g][q]);
+              if (real(k)) {
+                if (v > hv1) { hv2 = hv1; hv1 = v; hk = k; }
+                else hv2 = fmaxf(hv2, v);
+              }
+            }
+          errb = tol * cl1;
+          approx = true;
+        } else {
+          exact_alpha(i);
         }
       }
     }
@@ -233,24 +448,38 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G, int64_t 
   }
 }
 
+// Shared memory of one warp: Cholesky factor, alpha0 column, near-tie candidates.
 template <int KPL, int TMAX>
+__host__ __device__ constexpr int warp_smem_floats() {
+  return l_floats<TMAX>() + 32 * KPL + kMaxCand;
+}
+
+// Error allowance factor of the FP16 update from the coherence mu (as float bits, >= 0).
+__device__ __forceinline__ float h16_tolerance(const unsigned* mu_bits) {
+  return ldexpf(__uint_as_float(*mu_bits), -12) + ldexpf(1.f, -20);
+}
+
+template <int KPL, int TMAX, bool H16>
 __global__ void __launch_bounds__(kOmpWarps * 32, (TMAX <= 32 ? 3 : 2))
-omp_kernel(const float* __restrict__ G, int64_t ldg, const float* __restrict__ A0, int64_t lda,
-           int K, int64_t N, int T, const float* __restrict__ xnorm2,
+omp_kernel(const float* __restrict__ G, const uint16_t* __restrict__ Gh,
+           const unsigned* __restrict__ mu_bits, int64_t ldg, const float* __restrict__ A0,
+           int64_t lda, int K, int64_t N, int T, const float* __restrict__ xnorm2,
            const float* __restrict__ eps2, int32_t* __restrict__ idx_out,
            float* __restrict__ coef_out, int32_t* __restrict__ nnz_out, int* __restrict__ dev_err) {
   extern __shared__ __align__(16) float smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  float* L = smem + (size_t)wib * (l_floats<TMAX>() + 32 * KPL);   // Cholesky factor
+  float* L = smem + (size_t)wib * warp_smem_floats<KPL, TMAX>();   // Cholesky factor
   float* a0s = L + l_floats<TMAX>();                                // this warp's alpha0 column
+  int* cand = reinterpret_cast<int*>(a0s + 32 * KPL);
+  const float tol = H16 ? h16_tolerance(mu_bits) : 0.f;
   const int64_t warps_total = (int64_t)gridDim.x * kOmpWarps;
   bool numeric_bad = false;
   const bool emode = eps2 != nullptr;
   for (int64_t s = (int64_t)blockIdx.x * kOmpWarps + wib; s < N; s += warps_total)
-    omp_signal<KPL, TMAX>(G, ldg, A0 + s * lda, K, T, emode, emode ? eps2[s] : 0.f,
-                          emode ? xnorm2[s] : 0.f, idx_out + s * T, coef_out + s * T,
-                          nnz_out + s, L, a0s, numeric_bad);
+    omp_signal<KPL, TMAX, H16, false>(G, Gh, tol, ldg, A0 + s * lda, K, T, emode,
+                               emode ? eps2[s] : 0.f, emode ? xnorm2[s] : 0.f, idx_out + s * T,
+                               coef_out + s * T, nnz_out + s, L, a0s, cand, numeric_bad);
   if (__any_sync(KSVD_FULL_MASK, numeric_bad) && lane == 0) atomicOr(dev_err, kDevErrNumeric);
 }
 
@@ -268,8 +497,9 @@ omp_batched_kernel(const OmpJob* __restrict__ jobs, int njobs, int64_t total_chu
   extern __shared__ __align__(16) float smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  float* L = smem + (size_t)wib * (l_floats<TMAX>() + 32 * 32);
+  float* L = smem + (size_t)wib * warp_smem_floats<32, TMAX>();
   float* a0s = L + l_floats<TMAX>();
+  int* cand = reinterpret_cast<int*>(a0s + 32 * 32);
   bool numeric_bad = false;
   for (;;) {
     unsigned long long c = 0;
@@ -297,35 +527,27 @@ omp_batched_kernel(const OmpJob* __restrict__ jobs, int njobs, int64_t total_chu
       int32_t* io = jb.idx + s * jb.T;
       float* co = jb.coef + s * jb.T;
       switch (jb.kpl) {
-        case 4:
-          omp_signal<4, TMAX>(jb.G, jb.ldg, a0, jb.K, jb.T, emode, e2, xn2, io, co, jb.nnz + s, L,
-                              a0s, numeric_bad);
-          break;
-        case 8:
-          omp_signal<8, TMAX>(jb.G, jb.ldg, a0, jb.K, jb.T, emode, e2, xn2, io, co, jb.nnz + s, L,
-                              a0s, numeric_bad);
-          break;
-        case 16:
-          omp_signal<16, TMAX>(jb.G, jb.ldg, a0, jb.K, jb.T, emode, e2, xn2, io, co, jb.nnz + s,
-                               L, a0s, numeric_bad);
-          break;
-        default:
-          omp_signal<32, TMAX>(jb.G, jb.ldg, a0, jb.K, jb.T, emode, e2, xn2, io, co, jb.nnz + s,
-                               L, a0s, numeric_bad);
-          break;
+#define KSVD_BATCHED_SIGNAL(KPL)                                                              \
+  omp_signal<KPL, TMAX, false, true>(jb.G, nullptr, 0.f, jb.ldg, a0, jb.K, jb.T, emode, e2, xn2, \
+                                     io, co, jb.nnz + s, L, a0s, cand, numeric_bad)
+        case 4: KSVD_BATCHED_SIGNAL(4); break;
+        case 8: KSVD_BATCHED_SIGNAL(8); break;
+        case 16: KSVD_BATCHED_SIGNAL(16); break;
+        default: KSVD_BATCHED_SIGNAL(32); break;
+#undef KSVD_BATCHED_SIGNAL
       }
     }
   }
   if (__any_sync(KSVD_FULL_MASK, numeric_bad) && lane == 0) atomicOr(dev_err, kDevErrNumeric);
 }
 
-template <int KPL, int TMAX>
-cudaError_t launch_omp_t(const float* G, int64_t ldg, const float* A0, int64_t lda, int K,
-                         int64_t N, int T, const float* xnorm2, const float* eps2, int32_t* idx,
-                         float* coef, int32_t* nnz, int* dev_err, int grid_mult,
-                         cudaStream_t st) {
-  const size_t smem = (size_t)kOmpWarps * (l_floats<TMAX>() + 32 * KPL) * sizeof(float);
-  auto kern = omp_kernel<KPL, TMAX>;
+template <int KPL, int TMAX, bool H16>
+cudaError_t launch_omp_t(const float* G, const uint16_t* Gh, const unsigned* mu, int64_t ldg,
+                         const float* A0, int64_t lda, int K, int64_t N, int T,
+                         const float* xnorm2, const float* eps2, int32_t* idx, float* coef,
+                         int32_t* nnz, int* dev_err, int grid_mult, cudaStream_t st) {
+  const size_t smem = (size_t)kOmpWarps * warp_smem_floats<KPL, TMAX>() * sizeof(float);
+  auto kern = omp_kernel<KPL, TMAX, H16>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return e;
@@ -337,15 +559,15 @@ cudaError_t launch_omp_t(const float* G, int64_t ldg, const float* A0, int64_t l
   int64_t blocks = (N + kOmpWarps - 1) / kOmpWarps;
   const int64_t cap = (int64_t)sms * per_sm * (grid_mult > 0 ? grid_mult : 8);
   if (blocks > cap) blocks = cap;
-  kern<<<(unsigned)blocks, kOmpWarps * 32, smem, st>>>(G, ldg, A0, lda, K, N, T, xnorm2, eps2, idx,
-                                                       coef, nnz, dev_err);
+  kern<<<(unsigned)blocks, kOmpWarps * 32, smem, st>>>(G, Gh, mu, ldg, A0, lda, K, N, T, xnorm2,
+                                                       eps2, idx, coef, nnz, dev_err);
   return cudaGetLastError();
 }
 
 template <int TMAX>
 cudaError_t launch_omp_batched_t(const OmpJob* jobs, int njobs, int64_t total_chunks, int chunk,
                                  unsigned long long* queue, int* dev_err, cudaStream_t st) {
-  const size_t smem = (size_t)kOmpWarps * (l_floats<TMAX>() + 32 * 32) * sizeof(float);
+  const size_t smem = (size_t)kOmpWarps * warp_smem_floats<32, TMAX>() * sizeof(float);
   auto kern = omp_batched_kernel<TMAX>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
@@ -383,27 +605,71 @@ int omp_padded_k(int K) {
   return K <= 128 ? 128 : K <= 256 ? 256 : K <= 512 ? 512 : 1024;
 }
 
+// FP16 copy of G and the coherence mu = max_{i != j < K} |G(i, j)| (float bits, zeroed by the
+// caller), for the mixed path's alpha update.
+__global__ void gram_half_kernel(const float* __restrict__ G, int64_t ldg, int K, int64_t cols,
+                                 uint16_t* __restrict__ Gh, unsigned* __restrict__ mu_bits) {
+  const int64_t total = ldg * cols;
+  float mx = 0.f;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const float g = G[e];
+    Gh[e] = __half_as_ushort(__float2half_rn(g));
+    const int64_t col = e / ldg, row = e - col * ldg;
+    if (row < K && col < K && row != col) mx = fmaxf(mx, fabsf(g));
+  }
+  mx = warp_max(mx);
+  if ((threadIdx.x & 31) == 0 && mx > 0.f) atomicMax(mu_bits, __float_as_uint(mx));
+}
+
+cudaError_t launch_gram_half(const float* G, int64_t ldg, int K, uint16_t* Gh, unsigned* mu,
+                             cudaStream_t st) {
+  const int kp = omp_padded_k(K);
+  if (K < 1 || K > kMaxK || ldg < kp) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(mu, 0, sizeof(unsigned), st);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t need = (ldg * kp + 255) / 256;
+  const unsigned blocks = (unsigned)std::min<int64_t>(need, (int64_t)sms * 8);
+  gram_half_kernel<<<blocks, 256, 0, st>>>(G, ldg, K, kp, Gh, mu);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_omp(const float* G, int64_t ldg, const float* A0, int64_t lda, int K,
                        int64_t N, int T, const float* xnorm2, const float* eps2, int32_t* idx,
-                       float* coef, int32_t* nnz, int* dev_err, cudaStream_t st, int grid_mult) {
+                       float* coef, int32_t* nnz, int* dev_err, cudaStream_t st, int grid_mult,
+                       const uint16_t* Gh, const unsigned* mu) {
   if (N <= 0) return cudaSuccess;
   if (K < 1 || K > kMaxK || T < 1 || T > kMaxT) return cudaErrorInvalidValue;
   const int kp = omp_padded_k(K);   // the lanes touch rows [0, kp) of every column
   if (ldg < kp || lda < kp || (ldg & 3) || (lda & 3)) return cudaErrorInvalidValue;
-#define KSVD_OMP_ARGS G, ldg, A0, lda, K, N, T, xnorm2, eps2, idx, coef, nnz, dev_err, grid_mult, st
+  if ((Gh == nullptr) != (mu == nullptr)) return cudaErrorInvalidValue;
+  if (Gh && (ldg & 7)) return cudaErrorInvalidValue;   // 16-byte rows of eight FP16 values
+#define KSVD_OMP_ARGS G, Gh, mu, ldg, A0, lda, K, N, T, xnorm2, eps2, idx, coef, nnz, dev_err, \
+                      grid_mult, st
+  if (T <= 32 && Gh) {
+    switch (kp) {
+      case 128: return launch_omp_t<4, 32, true>(KSVD_OMP_ARGS);
+      case 256: return launch_omp_t<8, 32, true>(KSVD_OMP_ARGS);
+      case 512: return launch_omp_t<16, 32, true>(KSVD_OMP_ARGS);
+      default: return launch_omp_t<32, 32, true>(KSVD_OMP_ARGS);
+    }
+  }
   if (T <= 32) {
     switch (kp) {
-      case 128: return launch_omp_t<4, 32>(KSVD_OMP_ARGS);
-      case 256: return launch_omp_t<8, 32>(KSVD_OMP_ARGS);
-      case 512: return launch_omp_t<16, 32>(KSVD_OMP_ARGS);
-      default: return launch_omp_t<32, 32>(KSVD_OMP_ARGS);
+      case 128: return launch_omp_t<4, 32, false>(KSVD_OMP_ARGS);
+      case 256: return launch_omp_t<8, 32, false>(KSVD_OMP_ARGS);
+      case 512: return launch_omp_t<16, 32, false>(KSVD_OMP_ARGS);
+      default: return launch_omp_t<32, 32, false>(KSVD_OMP_ARGS);
     }
   }
   switch (kp) {
-    case 128: return launch_omp_t<4, 64>(KSVD_OMP_ARGS);
-    case 256: return launch_omp_t<8, 64>(KSVD_OMP_ARGS);
-    case 512: return launch_omp_t<16, 64>(KSVD_OMP_ARGS);
-    default: return launch_omp_t<32, 64>(KSVD_OMP_ARGS);
+    case 128: return launch_omp_t<4, 64, false>(KSVD_OMP_ARGS);
+    case 256: return launch_omp_t<8, 64, false>(KSVD_OMP_ARGS);
+    case 512: return launch_omp_t<16, 64, false>(KSVD_OMP_ARGS);
+    default: return launch_omp_t<32, 64, false>(KSVD_OMP_ARGS);
   }
 #undef KSVD_OMP_ARGS
 }

@@ -56,3 +56,73 @@ def test_mixed_iterations_match_fp64_rmse(oracle_mod, cuda, cfg, N, iters):
     idx, coef, nnz, rmse = h.iterate(Dd, to_dev(p["X"], cuda), iters, perms)
     np.testing.assert_allclose(rmse, rr, rtol=1e-2)
     h.close()
+
+
+def _coding_inputs(case):
+    """(G, alpha0, T, eps2-or-None) for the FP16 alpha update's selection test."""
+    rng = np.random.default_rng(77)
+    if case == "incoherent":
+        X, D = problem(256, 1024, 20000, 16, 42)
+        T = 16
+    elif case == "coherent":
+        X, D = problem(64, 256, 5000, 8, 43)
+        D[:, 128:] = D[:, :128] + 0.01 * rng.standard_normal((64, 128)).astype(np.float32)
+        D /= np.linalg.norm(D, axis=0)
+        T = 8
+    elif case == "noiseless":
+        D = rng.standard_normal((128, 512))
+        D /= np.linalg.norm(D, axis=0)
+        X = np.zeros((128, 5000))
+        for s in range(5000):
+            S = rng.choice(512, 6, replace=False)
+            X[:, s] = D[:, S] @ rng.standard_normal(6)
+        X, D = X.astype(np.float32), D.astype(np.float32)
+        T = 12
+    elif case == "ragged-K":
+        X, D = problem(100, 200, 5000, 10, 44)
+        T = 10
+    elif case == "t32":
+        X, D = problem(128, 512, 3000, 24, 45)
+        T = 32
+    else:  # error targets
+        X, D = problem(256, 1024, 10000, 16, 46)
+        T = 16
+    D64, X64 = D.astype(np.float64), X.astype(np.float64)
+    G = (D64.T @ D64).astype(np.float32)
+    A0 = (D64.T @ X64).astype(np.float32)
+    eps2 = None
+    if case == "eps":
+        xn = np.sum(X64 * X64, axis=0)
+        eps2 = (xn * rng.uniform(0.002, 0.05, X.shape[1])).astype(np.float32)
+    return X, G, A0, T, eps2
+
+
+@pytest.mark.parametrize("case", ["incoherent", "coherent", "noiseless", "ragged-K", "t32", "eps"])
+def test_fp16_alpha_update_selects_like_fp32(cuda, case):
+    """The mixed path's Batch-OMP forms alpha from an FP16 copy of G and re-evaluates every atom
+    within its error allowance of the maximum in FP32 with the FP32 path's operations.  Given the
+    same G and alpha0 its supports, coefficients and support sizes are bit-identical to the FP32
+    Batch-OMP's: on incoherent dictionaries (few near ties), on nearly duplicated atoms (many
+    candidates: the whole-alpha FP32 fallback), on noiseless signals (the stop tests at
+    exhaustion), at K not a multiple of 128, at T = 32 and with error targets."""
+    import torch
+
+    from ksvd_gb300 import Handle
+
+    X, G, A0, T, eps2 = _coding_inputs(case)
+    K = G.shape[0]
+    Gd, Ad = to_dev(G, cuda), to_dev(A0, cuda)
+    xn2 = e2 = None
+    if eps2 is not None:
+        xn2 = torch.from_numpy(np.sum(X.astype(np.float32) ** 2, axis=0)).to(cuda)
+        e2 = torch.from_numpy(eps2).to(cuda)
+    outs = []
+    for prec in ("fp32", "mixed"):
+        h = Handle(X.shape[0], K, T, precision=prec)
+        outs.append(h.omp_gram(Gd, Ad, xn2, e2))
+        h.synchronize()
+        h.close()
+    (ia, ca, na), (ib, cb, nb) = outs
+    assert torch.equal(na, nb)
+    assert torch.equal(ia, ib)
+    assert torch.equal(ca, cb)
