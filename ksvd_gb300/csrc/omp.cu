@@ -28,7 +28,8 @@ constexpr int kOmpWarps = 8;
 
 // Shared-memory layout of the Cholesky factor L (TMAX x TMAX, lower): rows of stride TMAX+1
 // (bank-conflict padding) up to TMAX = 32; for TMAX = 64 packed by rows (row r at r(r+1)/2),
-// half the space, so two CTAs fit on an SM.
+// half the space, so two CTAs fit on an SM.  The diagonal slots hold 1 / L_ii (the triangular
+// solves multiply instead of dividing).
 template <int TMAX>
 __host__ __device__ constexpr int l_floats() {
   return TMAX > 32 ? TMAX * (TMAX + 1) / 2 : TMAX * (TMAX + 1);
@@ -312,7 +313,7 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
         }
         for (int r = 0; r < i; ++r) {
           const int rl = r & 31, rj = r >> 5;
-          const float wr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(b, rj), rl) / L[lidx<TMAX>(r, r)];
+          const float wr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(b, rj), rl) * L[lidx<TMAX>(r, r)];
           if (lane == rl) put<SPL>(w, rj, wr);
 #pragma unroll
           for (int j = 0; j < SPL; ++j) {
@@ -337,7 +338,7 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
           if (q < i) L[lidx<TMAX>(i, q)] = w[j];
         }
       }
-      if (lane == 0) L[lidx<TMAX>(i, i)] = Lii;
+      if (lane == 0) L[lidx<TMAX>(i, i)] = 1.f / Lii;   // the solves multiply by 1 / L_ii
       if (lane == (i & 31)) { put<SPL>(ind, i >> 5, p); put<SPL>(y, i >> 5, ynew); }
       ++i;
       __syncwarp();
@@ -356,7 +357,7 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
         for (int j = 0; j < SPL; ++j) t[j] = y[j];
         for (int r = i - 1; r >= 0; --r) {
           const int rl = r & 31, rj = r >> 5;
-          const float cr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(t, rj), rl) / L[lidx<TMAX>(r, r)];
+          const float cr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(t, rj), rl) * L[lidx<TMAX>(r, r)];
           if (lane == rl) put<SPL>(c, rj, cr);
 #pragma unroll
           for (int j = 0; j < SPL; ++j) {
