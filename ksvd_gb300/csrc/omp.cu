@@ -104,8 +104,9 @@ constexpr int kMaxCand = 8;
 // H16 (mixed path): alpha = alpha0 - G(:, I) c is formed from an FP16 copy Gh of G (half the L2
 // bytes of the re-read support columns; c scaled by a power of two into FP16 range, products
 // accumulated in FP32).  Its error per atom is below 2^-10 sum_r |G(k, I_r) c_r|; the allowance
-// errb = tol * ||c||_1 (tol = 2^-12 mu + 2^-20, mu the dictionary's coherence) is a quarter of
-// that worst case and ~10x the rounding error's spread.  Every atom whose approximate |alpha|
+// errb = tol * ||c||_1 (tol = 2^-12 mu + 2^-18, mu the dictionary's coherence) is a quarter of
+// that worst case and ~10x the rounding error's spread; the 2^-18 floor covers FP16 subnormals
+// and the FP32 summation order.  Every atom whose approximate |alpha|
 // lies within 2 errb of the maximum is re-evaluated in FP32 with exactly the FP32 path's
 // operations, so the selection, the stop tests and the coefficients are those of the FP32
 // Batch-OMP; with more than kMaxCand candidates, or a maximum below 4 errb, the step's alpha is
@@ -369,25 +370,29 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
       // ---- alpha = alpha0 - G(:, I) c   (not needed after the last atom)
       if (i < T && !(emode && r2 <= e2)) {
         if constexpr (H16) {
-          float cmx = 0.f, cl1 = 0.f;
+          float cl1 = 0.f;
 #pragma unroll
           for (int j = 0; j < SPL; ++j)
-            if (lane + 32 * j < i) { cmx = fmaxf(cmx, fabsf(c[j])); cl1 += fabsf(c[j]); }
-          cmx = warp_max(cmx);
+            if (lane + 32 * j < i) cl1 += fabsf(c[j]);
           cl1 = warp_sum(cl1);
           int ex = 0;
-          frexpf(cmx, &ex);                    // |c| / 2^ex < 1: no FP16 overflow
+          frexpf(cl1, &ex);                    // |c| <= ||c||_1 < 2^ex: no FP16 overflow
           const float csc = ldexpf(1.f, ex), cisc = ldexpf(1.f, -ex);
 #pragma unroll
           for (int g = 0; g < NG; ++g)
 #pragma unroll
             for (int q = 0; q < V; ++q) al[g][q] = 0.f;
+          // slot r's scaled FP16 coefficient and atom, packed for one shuffle per column
+          // (H16 has one slot per lane: TMAX = 32)
+          const unsigned pack =
+              lane < i ? ((unsigned)__half_as_ushort(__float2half_rn(c[0] * cisc)) << 16) |
+                             (unsigned)ind[0]
+                       : 0u;
 #pragma unroll 1
           for (int r = 0; r < i; ++r) {
-            const int rl = r & 31, rj = r >> 5;
-            const float cr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(c, rj), rl);
-            const int col = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(ind, rj), rl);
-            const unsigned short ch = __half_as_ushort(__float2half_rn(cr * cisc));
+            const unsigned pk = __shfl_sync(KSVD_FULL_MASK, pack, r);
+            const unsigned short ch = (unsigned short)(pk >> 16);
+            const int col = (int)(pk & 0xffffu);
             const uint16_t* gp = Gh + (int64_t)col * ldg + V * lane;
 #pragma unroll
             for (int g = 0; g < NG; ++g) {
@@ -454,10 +459,20 @@ template <int KPL, int TMAX>
 __host__ __device__ constexpr int warp_smem_floats() {
   return l_floats<TMAX>() + 32 * KPL + kMaxCand;
 }
+// The same for supports of at most T atoms: L needs only its first T rows (a multiple of four
+// floats keeps the alpha0 column 16-byte aligned), so short supports leave room for more CTAs.
+template <int TMAX>
+__host__ __device__ constexpr int l_floats_for(int T) {
+  return (int)round_up(TMAX > 32 ? T * (T + 1) / 2 : T * (TMAX + 1), 4);
+}
+template <int KPL, int TMAX>
+__host__ __device__ constexpr int warp_smem_floats_for(int T) {
+  return l_floats_for<TMAX>(T) + 32 * KPL + kMaxCand;
+}
 
 // Error allowance factor of the FP16 update from the coherence mu (as float bits, >= 0).
 __device__ __forceinline__ float h16_tolerance(const unsigned* mu_bits) {
-  return ldexpf(__uint_as_float(*mu_bits), -12) + ldexpf(1.f, -20);
+  return ldexpf(__uint_as_float(*mu_bits), -12) + ldexpf(1.f, -18);
 }
 
 template <int KPL, int TMAX, bool H16>
@@ -470,8 +485,8 @@ omp_kernel(const float* __restrict__ G, const uint16_t* __restrict__ Gh,
   extern __shared__ __align__(16) float smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  float* L = smem + (size_t)wib * warp_smem_floats<KPL, TMAX>();   // Cholesky factor
-  float* a0s = L + l_floats<TMAX>();                                // this warp's alpha0 column
+  float* L = smem + (size_t)wib * warp_smem_floats_for<KPL, TMAX>(T);   // Cholesky factor
+  float* a0s = L + l_floats_for<TMAX>(T);                                // alpha0 column
   int* cand = reinterpret_cast<int*>(a0s + 32 * KPL);
   const float tol = H16 ? h16_tolerance(mu_bits) : 0.f;
   const int64_t warps_total = (int64_t)gridDim.x * kOmpWarps;
@@ -547,7 +562,7 @@ cudaError_t launch_omp_t(const float* G, const uint16_t* Gh, const unsigned* mu,
                          const float* A0, int64_t lda, int K, int64_t N, int T,
                          const float* xnorm2, const float* eps2, int32_t* idx, float* coef,
                          int32_t* nnz, int* dev_err, int grid_mult, cudaStream_t st) {
-  const size_t smem = (size_t)kOmpWarps * warp_smem_floats<KPL, TMAX>() * sizeof(float);
+  const size_t smem = (size_t)kOmpWarps * warp_smem_floats_for<KPL, TMAX>(T) * sizeof(float);
   auto kern = omp_kernel<KPL, TMAX, H16>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
