@@ -133,11 +133,15 @@ def stage_flops(cfg, N, stage):
 # DRAM bytes per signal of one launch, from ncu captures (dram__bytes_read.sum +
 # dram__bytes_write.sum) of the same kernel on 100,000 signals of the same (n, K, T); traffic grows
 # in proportion to the signals, so the bench scales it to its N.  profiles/omp_kernel_cfg2.md.
-MEASURED_TRAFFIC = {("omp", 256, 1024, 16): (414.144256e6 + 7.270400e6) / 100_000}
+# Keyed by (stage, n, K, T, precision): the mixed path runs the FP16-update Batch-OMP kernel.
+MEASURED_TRAFFIC = {("omp", 256, 1024, 16, "fp32"): (414.167808e6 + 7.126272e6) / 100_000,
+                    ("omp", 256, 1024, 16, "mixed"): (416.039680e6 + 7.574528e6) / 100_000}
 
-# The unit that binds Batch-OMP is L2 (G's support columns re-read every step): L2 throughput in
-# percent of peak (lts__throughput.avg.pct_of_peak_sustained_elapsed) from the same capture.
-MEASURED_L2_PCT = {("omp", 256, 1024, 16): 69.75}
+# Batch-OMP re-reads G's support columns from L2 every step: L2 throughput in percent of peak
+# (lts__throughput.avg.pct_of_peak_sustained_elapsed) and issue-active percent from the same
+# captures -- the FP32 kernel is bound by L2, the FP16-update kernel by instruction issue.
+MEASURED_L2_PCT = {("omp", 256, 1024, 16, "fp32"): (77.16, 52.73),
+                   ("omp", 256, 1024, 16, "mixed"): (47.63, 67.88)}
 
 # FP32 CUDA-core peak (nominal): 152 SMs x 128 FMA lanes x 2 FLOP x 2.07 GHz.
 FP32_SIMT_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
@@ -600,7 +604,7 @@ def main():
         ach = stage_bytes(cfg, N, dom) / (launch_ms / 1e3) / 1e9
         roof = {"bound": "hbm", "achieved": ach, "peak": pk["hbm"], "unit": "GB/s",
                 "frac": ach / pk["hbm"], "traffic": None}
-    tpu = MEASURED_TRAFFIC.get((dom, cfg.n, cfg.K, cfg.T))
+    tpu = MEASURED_TRAFFIC.get((dom, cfg.n, cfg.K, cfg.T, args.precision))
     if tpu is not None and roof["bound"] == "hbm":
         roof["traffic"] = tpu * N
         roof["traffic_source"] = "ncu capture at N=100000, scaled by N"
@@ -610,11 +614,14 @@ def main():
         tf = fl / (launch_ms / 1e3) / 1e12
         roof["compute"] = {"achieved": tf, "peak": FP32_SIMT_TFLOPS, "unit": "TFLOP/s",
                            "frac": tf / FP32_SIMT_TFLOPS, "peak_source": "nominal FP32 SIMT"}
-        l2 = MEASURED_L2_PCT.get((dom, cfg.n, cfg.K, cfg.T))
+        l2 = MEASURED_L2_PCT.get((dom, cfg.n, cfg.K, cfg.T, args.precision))
         if l2 is not None:
-            roof["l2"] = {"throughput_pct_of_peak": l2,
-                          "source": "ncu lts__throughput at N=100000 (profiles/omp_kernel_cfg2.md)",
-                          "support_column_bytes": float(N) * cfg.K * 4 * cfg.T * (cfg.T - 1) / 2}
+            gbytes = 2 if args.precision == "mixed" else 4
+            roof["l2"] = {"throughput_pct_of_peak": l2[0], "issue_active_pct": l2[1],
+                          "source": "ncu lts__throughput / smsp__issue_active at N=100000 "
+                                    "(profiles/omp_kernel_cfg2.md)",
+                          "support_column_bytes":
+                              float(N) * cfg.K * gbytes * cfg.T * (cfg.T - 1) / 2}
     roof["kernel"] = dom
     roof["peak_source"] = pk["src"]
     stage_summary = {k: {"ms_per_launch": round(v[0], 4), "share": round(v[0] * v[1] / sum(
