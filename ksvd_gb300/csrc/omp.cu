@@ -208,10 +208,11 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
     int i = 0;
     bool approx = false;   // al holds the FP16 update's alpha
     float errb = 0.f;      // its error allowance per atom
-    // this lane's two largest approximate |alpha| (with the first maximum's atom), formed by the
-    // FP16 update's last pass
-    float hv1 = -1.f, hv2 = -1.f;
-    int hk = 0x7fffffff;
+    // this lane's two largest approximate |alpha| as keys, formed by the FP16 update's last pass:
+    // the bits of |alpha| (positive floats order like unsigned integers) with the low five
+    // mantissa bits replaced by 31 - (the element's slot in the lane), so one unsigned max tracks
+    // value and atom together (the truncation, < 2^-18 relative, joins the tie allowance)
+    unsigned hk1 = 0u, hk2 = 0u;
     while (i < T) {
       if (emode && r2 <= e2) break;
       float bv;
@@ -221,22 +222,22 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
         if (approx) {
           approx = false;
           // warp maximum and runner-up of the approximate |alpha|
-          float b2 = hv2, b1 = hv1;
-          bk = hk;
+          unsigned c1 = hk1, c2 = hk2;
 #pragma unroll
           for (int o = 16; o > 0; o >>= 1) {
-            const float ov = __shfl_xor_sync(KSVD_FULL_MASK, b1, o);
-            const int ok = __shfl_xor_sync(KSVD_FULL_MASK, bk, o);
-            const float o2 = __shfl_xor_sync(KSVD_FULL_MASK, b2, o);
-            if (ov > b1 || (ov == b1 && ok < bk)) {
-              b2 = fmaxf(b1, o2); b1 = ov; bk = ok;
-            } else {
-              b2 = fmaxf(b2, ov);
-            }
+            const unsigned o1 = __shfl_xor_sync(KSVD_FULL_MASK, c1, o);
+            const unsigned o2 = __shfl_xor_sync(KSVD_FULL_MASK, c2, o);
+            c2 = max(max(c2, o2), min(c1, o1));
+            c1 = max(c1, o1);
           }
+          const int wl = __ffs(__ballot_sync(KSVD_FULL_MASK, hk1 == c1)) - 1;
+          const int wb = 31 - (int)(c1 & 31u);
+          bk = 32 * V * (wb / V) + V * wl + (wb % V);
+          const float b1 = __uint_as_float(c1 & 0x7FFFFFE0u);
+          const float b2 = __uint_as_float(c2 & 0x7FFFFFE0u);
           bv = b1 * b1;
-          const float thr = b1 - 2.f * errb;
-          bool full = !(b1 > 4.f * errb) || !(b1 > 1e-6f);
+          const float thr = b1 - 2.f * errb - ldexpf(b1, -17);
+          bool full = !(b1 > 4.f * errb) || !(b1 > 1e-6f) || !(b1 <= 3.0e38f);
           if (!full && !(b2 < thr)) {
             // near tie: every atom within 2 errb of the maximum is a candidate
             unsigned mine = 0;
@@ -409,7 +410,7 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
               }
             }
           }
-          hv1 = -1.f; hv2 = -1.f; hk = 0x7fffffff;
+          hk1 = 0u; hk2 = 0u;
 #pragma unroll
           for (int g = 0; g < NG; ++g)
 #pragma unroll
@@ -425,11 +426,10 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
           for (int g = 0; g < NG; ++g)
 #pragma unroll
             for (int q = 0; q < V; ++q) {
-              const int k = 32 * V * g + V * lane + q;
-              const float v = fabsf(al[g][q]);
-              if (real(k)) {
-                if (v > hv1) { hv2 = hv1; hv1 = v; hk = k; }
-                else hv2 = fmaxf(hv2, v);
+              const unsigned key = (__float_as_uint(al[g][q]) & 0x7FFFFFE0u) | (31u - (V * g + q));
+              if (real(32 * V * g + V * lane + q)) {
+                hk2 = max(hk2, min(hk1, key));
+                hk1 = max(hk1, key);
               }
             }
           errb = tol * cl1;
