@@ -59,6 +59,11 @@ __device__ __forceinline__ int pick(const int (&a)[SPL], int j) {
   if constexpr (SPL == 1) return a[0];
   else return j == 0 ? a[0] : a[1];
 }
+template <int SPL>
+__device__ __forceinline__ unsigned pick(const unsigned (&a)[SPL], int j) {
+  if constexpr (SPL == 1) return a[0];
+  else return j == 0 ? a[0] : a[1];
+}
 template <int SPL, typename V>
 __device__ __forceinline__ void put(V (&a)[SPL], int j, V v) {
   if constexpr (SPL == 1) a[0] = v;
@@ -111,7 +116,7 @@ constexpr int kMaxCand = 8;
 // operations, so the selection, the stop tests and the coefficients are those of the FP32
 // Batch-OMP; with more than kMaxCand candidates, or a maximum below 4 errb, the step's alpha is
 // recomputed in FP32.
-template <int KPL, int TMAX, bool H16, bool CHECKK>
+template <int KPL, int TMAX, bool H16>
 __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
                                            const uint16_t* __restrict__ Gh, float tol,
                                            int64_t ldg, const float* __restrict__ a0col, int K,
@@ -124,12 +129,10 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
   constexpr int V = (H16 && KPL >= 8) ? 8 : 4;
   constexpr int NG = KPL / V;
   constexpr int SPL = TMAX / 32; // support slots per lane; lane owns slots lane + 32*j
-  static_assert(!H16 || TMAX == 32, "the FP16 update serves supports of up to 32 atoms");
   const int lane = threadIdx.x & 31;
-  // rows >= K of G and alpha0 are zero, so their alpha stays 0 (or NaN) and never wins a strict
-  // comparison against the first real atom; CHECKK keeps the explicit test for callers whose
-  // padding is not guaranteed
-  auto real = [&](int k) { return !CHECKK || k < K; };
+  // Rows >= K of G and alpha0 are zero (every caller pads them), so the padded atoms' alpha
+  // stays 0 (or NaN) and never wins a strict comparison against the first real atom: the
+  // per-element passes need no k < K test.
   {
     float al[NG][V];
     const float* a0p = a0col + V * lane;
@@ -194,7 +197,7 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
         for (int q = 0; q < V; ++q) {
           const int k = 32 * V * g + V * lane + q;
           const float v = al[g][q] * al[g][q];
-          if (real(k) && v > bv) { bv = v; bk = k; }
+          if (v > bv) { bv = v; bk = k; }
         }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
@@ -246,7 +249,7 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
 #pragma unroll
               for (int q = 0; q < V; ++q) {
                 const int k = 32 * V * g + V * lane + q;
-                if (real(k) && fabsf(al[g][q]) >= thr) mine |= 1u << (V * g + q);
+                if (fabsf(al[g][q]) >= thr) mine |= 1u << (V * g + q);
               }
             const int cnt = __popc(mine);
             int incl = cnt;
@@ -384,14 +387,16 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
 #pragma unroll
             for (int q = 0; q < V; ++q) al[g][q] = 0.f;
           // slot r's scaled FP16 coefficient and atom, packed for one shuffle per column
-          // (H16 has one slot per lane: TMAX = 32)
-          const unsigned pack =
-              lane < i ? ((unsigned)__half_as_ushort(__float2half_rn(c[0] * cisc)) << 16) |
-                             (unsigned)ind[0]
-                       : 0u;
+          unsigned pack[SPL];
+#pragma unroll
+          for (int j = 0; j < SPL; ++j)
+            pack[j] = lane + 32 * j < i
+                          ? ((unsigned)__half_as_ushort(__float2half_rn(c[j] * cisc)) << 16) |
+                                (unsigned)ind[j]
+                          : 0u;
 #pragma unroll 1
           for (int r = 0; r < i; ++r) {
-            const unsigned pk = __shfl_sync(KSVD_FULL_MASK, pack, r);
+            const unsigned pk = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(pack, r >> 5), r & 31);
             const unsigned short ch = (unsigned short)(pk >> 16);
             const int col = (int)(pk & 0xffffu);
             const uint16_t* gp = Gh + (int64_t)col * ldg + V * lane;
@@ -427,10 +432,8 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
 #pragma unroll
             for (int q = 0; q < V; ++q) {
               const unsigned key = (__float_as_uint(al[g][q]) & 0x7FFFFFE0u) | (31u - (V * g + q));
-              if (real(32 * V * g + V * lane + q)) {
-                hk2 = max(hk2, min(hk1, key));
-                hk1 = max(hk1, key);
-              }
+              hk2 = max(hk2, min(hk1, key));
+              hk1 = max(hk1, key);
             }
           errb = tol * cl1;
           approx = true;
@@ -493,7 +496,7 @@ omp_kernel(const float* __restrict__ G, const uint16_t* __restrict__ Gh,
   bool numeric_bad = false;
   const bool emode = eps2 != nullptr;
   for (int64_t s = (int64_t)blockIdx.x * kOmpWarps + wib; s < N; s += warps_total)
-    omp_signal<KPL, TMAX, H16, false>(G, Gh, tol, ldg, A0 + s * lda, K, T, emode,
+    omp_signal<KPL, TMAX, H16>(G, Gh, tol, ldg, A0 + s * lda, K, T, emode,
                                emode ? eps2[s] : 0.f, emode ? xnorm2[s] : 0.f, idx_out + s * T,
                                coef_out + s * T, nnz_out + s, L, a0s, cand, numeric_bad);
   if (__any_sync(KSVD_FULL_MASK, numeric_bad) && lane == 0) atomicOr(dev_err, kDevErrNumeric);
@@ -544,8 +547,8 @@ omp_batched_kernel(const OmpJob* __restrict__ jobs, int njobs, int64_t total_chu
       float* co = jb.coef + s * jb.T;
       switch (jb.kpl) {
 #define KSVD_BATCHED_SIGNAL(KPL)                                                              \
-  omp_signal<KPL, TMAX, false, true>(jb.G, nullptr, 0.f, jb.ldg, a0, jb.K, jb.T, emode, e2, xn2, \
-                                     io, co, jb.nnz + s, L, a0s, cand, numeric_bad)
+  omp_signal<KPL, TMAX, false>(jb.G, nullptr, 0.f, jb.ldg, a0, jb.K, jb.T, emode, e2, xn2, io, \
+                               co, jb.nnz + s, L, a0s, cand, numeric_bad)
         case 4: KSVD_BATCHED_SIGNAL(4); break;
         case 8: KSVD_BATCHED_SIGNAL(8); break;
         case 16: KSVD_BATCHED_SIGNAL(16); break;
