@@ -231,9 +231,13 @@ typedef struct ksvd_tuning {
                                their own streams with SM shares; 0 (default) = one after
                                another, each sweep on the whole GPU                            */
   int32_t tuned;         /* 1 after an autotune call                                           */
+  int32_t omp_fp16;      /* mixed precision, T <= 32: Batch-OMP's alpha update from an FP16 copy
+                            of G with FP32 near-tie re-evaluation (same selections as FP32):
+                            1 on, 0 off, -1 automatic (on for T >= 14)                        */
 } ksvd_tuning;
 
-/* Times Batch-OMP grid sizes and sweep CTA counts on this problem (D n x K, X n x N, device) and
+/* Times Batch-OMP grid sizes (and, for a mixed-precision handle, the FP16 alpha update on and
+ * off) and sweep CTA counts on this problem (D n x K, X n x N, device) and
  * keeps the fastest for the handle's later calls; D, X and the atom-order stream are not
  * changed.  Costs a few OMP and dictionary-update passes.  No reference counterpart. */
 KSVD_API ksvd_status ksvd_autotune(ksvd_handle* handle, const float* D, const float* X, int64_t N,

@@ -59,7 +59,7 @@ class Tuning(C.Structure):
     """ksvd_tuning: launch shapes chosen per handle."""
     _fields_ = [("omp_grid_mult", C.c_int32), ("sweep_ctas", C.c_int32),
                 ("batch_chunk", C.c_int32), ("batch_concurrent", C.c_int32),
-                ("tuned", C.c_int32)]
+                ("tuned", C.c_int32), ("omp_fp16", C.c_int32)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}

@@ -150,7 +150,9 @@ class Handle:
 
     @tuning.setter
     def tuning(self, d):
-        t = _native.Tuning(**{k: int(v) for k, v in d.items()})
+        cur = self.tuning                  # keys left out keep their current values
+        cur.update({k: int(v) for k, v in d.items()})
+        t = _native.Tuning(**cur)
         self._check(self._lib.ksvd_set_tuning(self._h, C.byref(t)))
 
     def graph_replays(self) -> int:

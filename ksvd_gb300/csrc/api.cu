@@ -85,6 +85,7 @@ struct ksvd_handle {
     cudaEvent_t dev_ev[2] = {};
   } inflow;
   int omp_grid_mult = 0;  // Batch-OMP blocks per resident CTA slot (0: default)
+  int omp_fp16 = -1;      // mixed path's FP16 alpha update: 1 on, 0 off, -1 automatic
   int batch_chunk = 0;    // signals per batched work-queue chunk (0: default)
   int batch_concurrent = 0;  // batched updates: 1 = concurrent streams with SM shares,
                              // 0 = one after another, each sweep on the whole GPU
@@ -341,10 +342,13 @@ ksvd_status run_omp(ksvd_handle* h, const float* G, const float* A0, int64_t N,
   int* de = nullptr;
   KSVD_TRY(ensure(h, B_DEVERR, 1, &de));
   // mixed path: the alpha update reads an FP16 copy of G (made here, G may have changed since
-  // the last call) and resolves near ties in FP32
+  // the last call) and resolves near ties in FP32.  It pays once the re-read support columns
+  // dominate the step (measured: slower at T = 8 and 10, faster at T = 16); the autotuner
+  // times both.
   uint16_t* gh = nullptr;
   unsigned* mu = nullptr;
-  if (mixed(h) && h->p.T <= 32) {
+  const int T = h->p.T;
+  if (mixed(h) && T <= 32 && (h->omp_fp16 > 0 || (h->omp_fp16 < 0 && T >= 14))) {
     KSVD_TRY(ensure(h, B_GH, (size_t)h->Kp * h->Kp, &gh));
     KSVD_TRY(ensure(h, B_MU, 1, &mu));
   }
@@ -941,6 +945,7 @@ void fill_tuning(const ksvd_handle* h, ksvd_tuning* out) {
   out->batch_chunk = h->batch_chunk;
   out->batch_concurrent = h->batch_concurrent;
   out->tuned = h->tuned ? 1 : 0;
+  out->omp_fp16 = h->omp_fp16;
 }
 
 }  // namespace
@@ -978,17 +983,24 @@ ksvd_status ksvd_autotune(ksvd_handle* h, const float* D, const float* X, int64_
   h->p.flags &= ~KSVD_FLAG_PROFILE;        // no stage events while tuning
   ksvd_status st = KSVD_OK;
   double best = 1e30;
-  int best_mult = 8;
-  for (int mult : {1, 2, 4, 8, 16}) {
-    h->omp_grid_mult = mult;
-    double ms = 0;
-    st = time_on_stream(h, 3, [&] {
-      return run_omp(h, G, A0, N, nullptr, nullptr, idx, coef, nnz);
-    }, &ms);
+  int best_mult = 8, best_fp16 = h->omp_fp16;
+  const bool try_fp16 = mixed(h) && T <= 32;
+  for (int fp16 : {0, 1}) {
+    if (!try_fp16 && fp16 == 1) break;
+    if (try_fp16) h->omp_fp16 = fp16;
+    for (int mult : {1, 2, 4, 8, 16}) {
+      h->omp_grid_mult = mult;
+      double ms = 0;
+      st = time_on_stream(h, 3, [&] {
+        return run_omp(h, G, A0, N, nullptr, nullptr, idx, coef, nnz);
+      }, &ms);
+      if (st != KSVD_OK) break;
+      if (ms < best) { best = ms; best_mult = mult; best_fp16 = h->omp_fp16; }
+    }
     if (st != KSVD_OK) break;
-    if (ms < best) { best = ms; best_mult = mult; }
   }
   h->omp_grid_mult = best_mult;
+  h->omp_fp16 = best_fp16;
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
   const int64_t draws = h->perm_draws;
@@ -1098,8 +1110,9 @@ ksvd_status ksvd_get_tuning(const ksvd_handle* h, ksvd_tuning* out) {
 
 ksvd_status ksvd_set_tuning(ksvd_handle* h, const ksvd_tuning* t) {
   if (!h || !t || t->omp_grid_mult < 0 || t->omp_grid_mult > 64 || t->sweep_ctas < 0 ||
-      t->batch_chunk < 0 || t->batch_chunk > 4096)
+      t->batch_chunk < 0 || t->batch_chunk > 4096 || t->omp_fp16 < -1 || t->omp_fp16 > 1)
     return KSVD_ERR_INVALID_ARGUMENT;
+  h->omp_fp16 = t->omp_fp16;
   h->omp_grid_mult = t->omp_grid_mult;
   h->sweep_ctas = t->sweep_ctas;
   h->batch_chunk = t->batch_chunk;

@@ -119,6 +119,8 @@ def test_fp16_alpha_update_selects_like_fp32(cuda, case):
     outs = []
     for prec in ("fp32", "mixed"):
         h = Handle(X.shape[0], K, T, precision=prec)
+        if prec == "mixed":
+            h.tuning = dict(h.tuning, omp_fp16=1)     # the FP16 update at every T
         outs.append(h.omp_gram(Gd, Ad, xn2, e2))
         h.synchronize()
         h.close()
