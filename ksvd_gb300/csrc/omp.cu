@@ -101,21 +101,20 @@ __device__ __forceinline__ void fma2_f16_f32(uint32_t g, unsigned short c, float
 // per step; more candidates (or a maximum too small to trust) recompute the whole alpha in FP32.
 constexpr int kMaxCand = 8;
 
-// Batch-OMP of one signal by one warp.  a0p: the signal's alpha0 column (Kp = 32*KPL rows, rows
-// >= K zero); L: (TMAX x TMAX+1) and a0s: (32*KPL) floats, cand: kMaxCand ints of this warp's
-// shared memory.  emode: stop once ||x||^2 - ||y||^2 <= e2 (xn2 = ||x||^2).  Writes T slots of
-// idx/coef and nnz.
+// Batch-OMP of one signal by one warp.  a0col: the signal's alpha0 column (Kp = 32*KPL rows,
+// rows >= K zero); L: the Cholesky factor (first T rows of the TMAX layout), a0s: 32*KPL floats
+// and cand: kMaxCand ints of this warp's shared memory.  emode: stop once ||x||^2 - ||y||^2 <= e2
+// (xn2 = ||x||^2).  Writes T slots of idx/coef and nnz.
 //
 // H16 (mixed path): alpha = alpha0 - G(:, I) c is formed from an FP16 copy Gh of G (half the L2
 // bytes of the re-read support columns; c scaled by a power of two into FP16 range, products
 // accumulated in FP32).  Its error per atom is below 2^-10 sum_r |G(k, I_r) c_r|; the allowance
 // errb = tol * ||c||_1 (tol = 2^-12 mu + 2^-18, mu the dictionary's coherence) is a quarter of
 // that worst case and ~10x the rounding error's spread; the 2^-18 floor covers FP16 subnormals
-// and the FP32 summation order.  Every atom whose approximate |alpha|
-// lies within 2 errb of the maximum is re-evaluated in FP32 with exactly the FP32 path's
-// operations, so the selection, the stop tests and the coefficients are those of the FP32
-// Batch-OMP; with more than kMaxCand candidates, or a maximum below 4 errb, the step's alpha is
-// recomputed in FP32.
+// and the FP32 summation order.  Every atom whose approximate |alpha| lies within 2 errb of the
+// maximum is re-evaluated in FP32 with exactly the FP32 path's operations, so the selection, the
+// stop tests and the coefficients are those of the FP32 Batch-OMP; with more than kMaxCand
+// candidates, or a maximum below 4 errb, the step's alpha is recomputed in FP32.
 template <int KPL, int TMAX, bool H16>
 __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
                                            const uint16_t* __restrict__ Gh, float tol,
