@@ -81,6 +81,9 @@ def _coding_inputs(case):
     elif case == "ragged-K":
         X, D = problem(100, 200, 5000, 10, 44)
         T = 10
+    elif case == "small-K":
+        X, D = problem(64, 100, 3000, 10, 48)
+        T = 16
     elif case == "t32":
         X, D = problem(128, 512, 3000, 24, 45)
         T = 32
@@ -97,14 +100,16 @@ def _coding_inputs(case):
     return X, G, A0, T, eps2
 
 
-@pytest.mark.parametrize("case", ["incoherent", "coherent", "noiseless", "ragged-K", "t32", "eps"])
+@pytest.mark.parametrize("case", ["incoherent", "coherent", "noiseless", "ragged-K", "small-K",
+                                  "t32", "eps"])
 def test_fp16_alpha_update_selects_like_fp32(cuda, case):
     """The mixed path's Batch-OMP forms alpha from an FP16 copy of G and re-evaluates every atom
     within its error allowance of the maximum in FP32 with the FP32 path's operations.  Given the
     same G and alpha0 its supports, coefficients and support sizes are bit-identical to the FP32
     Batch-OMP's: on incoherent dictionaries (few near ties), on nearly duplicated atoms (many
     candidates: the whole-alpha FP32 fallback), on noiseless signals (the stop tests at
-    exhaustion), at K not a multiple of 128, at T = 32 and with error targets."""
+    exhaustion), at K not a multiple of 128 (also K <= 128: four rows per lane and group), at
+    T = 32 and with error targets."""
     import torch
 
     from ksvd_gb300 import Handle
