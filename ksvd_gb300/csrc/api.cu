@@ -1024,7 +1024,7 @@ ksvd_status ksvd_autotune(ksvd_handle* h, const float* D, const float* X, int64_
   if (st == KSVD_OK) st = upload_perm(h, nullptr, 1, &pd);
   best = 1e30;
   int best_ctas = 0;
-  for (int div : {1, 2, 4}) {
+  for (int div : {1, 2, 4, 8, 16}) {
     if (st != KSVD_OK) break;
     const int ctas = std::max(1, sms / div);
     h->sweep_ctas = ctas;

@@ -765,6 +765,8 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
   const int K = A.K, n = A.n, tid = threadIdx.x;
   constexpr int HALF = Sweep<NPL>::HALF;
   const int32_t* perm = A.perm + (A.iter_ctr ? (int64_t)(*A.iter_ctr) * K : 0);
+  // fewer than ~50 list entries per atom and CTA on average (measured: 26 faster, 103 slower)
+  const bool light = A.N * A.T < 50LL * K * gridDim.x;
   // every CTA checks the whole permutation itself, so all of them leave together or none does
   int bad = 0;
   for (int k = tid; k < A.Kp; k += blockDim.x) S.pos[k] = K;   // (an order with repeats: no skips)
@@ -819,12 +821,16 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
       constexpr int QUART = HALF / 2;
       if (S.c == 0)
         for (int r = gt; r < n; r += HALF) A.D[(int64_t)j * n + r] = S.a_s[r] / anorm;
+      // With few signals per atom and CTA the helpers set the phase's length, and the prefetch
+      // goes with the shorter refresh task; with many, the coefficient warps do, and the
+      // prefetch (whose lines the next phase reads) stays after the partials.
       if (gt < QUART) {
         S.refresh_gp(j, 1.f / anorm, true, gt, QUART);
+        if (light && jn >= 0) S.prefetch_next(jn, (jj + 1) & 1, gt, QUART);
       } else if (jn >= 0) {
         S.next_partials(jn, j, av_next, ad_next, gt - QUART, QUART);
         S.zero_row(jn, gt - QUART, QUART);
-        S.prefetch_next(jn, (jj + 1) & 1, gt - QUART, QUART);
+        if (!light) S.prefetch_next(jn, (jj + 1) & 1, gt - QUART, QUART);
       }
       S.update_coefs(j, q0, cnt, anorm, jj & 1, &next_batch, &use_cnt);
     }
