@@ -280,7 +280,8 @@ def test_iterate_host_matches_device(oracle_mod, cuda, N, precision, iters):
         # one iteration: the drained code is the device code, up to the sweep's atomics
         assert rel_rmse(ch, coef.cpu().numpy()) < 1e-5
     # the atom sweep accumulates with float atomics, so two runs agree to rounding, not bitwise
-    np.testing.assert_allclose(rh, rd, rtol=1e-6)
+    # (after the second iteration's coding, to ~1e-6 relative)
+    np.testing.assert_allclose(rh, rd, rtol=1e-5)
     assert support_match_vec(ih, nh, idx.cpu().numpy(), nnz.cpu().numpy()) >= SUPPORT_MIN
     # the sweep's float atomics reorder sums run to run; with more signals a coefficient can
     # land on the other side of a near-tie in the second iteration's coding
