@@ -81,6 +81,10 @@ def _coding_inputs(case):
     elif case == "ragged-K":
         X, D = problem(100, 200, 5000, 10, 44)
         T = 10
+    elif case in ("scale-up", "scale-down"):
+        X, D = problem(128, 512, 3000, 12, 49)
+        X = X * np.float32(1e4 if case == "scale-up" else 1e-4)   # coefficients far from 1
+        T = 16
     elif case == "small-K":
         X, D = problem(64, 100, 3000, 10, 48)
         T = 16
@@ -101,14 +105,15 @@ def _coding_inputs(case):
 
 
 @pytest.mark.parametrize("case", ["incoherent", "coherent", "noiseless", "ragged-K", "small-K",
-                                  "t32", "eps"])
+                                  "scale-up", "scale-down", "t32", "eps"])
 def test_fp16_alpha_update_selects_like_fp32(cuda, case):
     """The mixed path's Batch-OMP forms alpha from an FP16 copy of G and re-evaluates every atom
     within its error allowance of the maximum in FP32 with the FP32 path's operations.  Given the
     same G and alpha0 its supports, coefficients and support sizes are bit-identical to the FP32
     Batch-OMP's: on incoherent dictionaries (few near ties), on nearly duplicated atoms (many
     candidates: the whole-alpha FP32 fallback), on noiseless signals (the stop tests at
-    exhaustion), at K not a multiple of 128 (also K <= 128: four rows per lane and group), at
+    exhaustion), at K not a multiple of 128 (also K <= 128: four rows per lane and group), with
+    signals scaled by 1e4 and 1e-4 (the coefficients' power-of-two scaling into FP16 range), at
     T = 32 and with error targets."""
     import torch
 
