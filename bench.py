@@ -315,7 +315,7 @@ def cpu_baseline_batched(probs, per_problem):
 def run_batched(args):
     """The batched workload: 64 independent dictionaries (n in {32, 64, 128, 256}, K = 4n,
     N in 10k..200k, error-constrained supports of 1..64 atoms); one step = one K-SVD iteration
-    of every problem (persistent Batch-OMP launches + the per-problem updates)."""
+    of every problem (one persistent Batch-OMP launch + concurrent per-problem updates)."""
     import numpy as np
     import torch
 

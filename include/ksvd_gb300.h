@@ -267,17 +267,16 @@ typedef struct ksvd_problem {
   int32_t* nnz;       /* N atoms used per signal (out)                                       */
 } ksvd_problem;
 
-/* Batch-OMP of every problem: one grouped GEMM launch for all G = D'D and alpha0 = D'X, then
- * one persistent launch per atom-padding class (Kp = 128, 256, 512, 1024; at most four) in which
- * warps take chunks of signals of any problem of the class from a device work queue (uneven
- * supports from the error targets balance themselves).  FP32; the handle's
+/* Batch-OMP of every problem: one grouped GEMM launch for all G = D'D and alpha0 = D'X, then ONE
+ * persistent launch in which warps take chunks of signals of any problem from a device work
+ * queue (uneven supports from the error targets balance themselves).  FP32; the handle's
  * n/K/T are not used, only its stream and workspace.  Asynchronous on the handle's stream.
  * Replaces a loop of OMP::BatchOMP calls (S/OMP.cu:42-59), one per dictionary. */
 KSVD_API ksvd_status ksvd_batched_omp(ksvd_handle* handle, const ksvd_problem* probs,
                                       int32_t nprob);
 
-/* iters K-SVD iterations of every problem (each N >= 1): per iteration the persistent Batch-OMP
- * launches over all problems (as ksvd_batched_omp), then every problem's dictionary update, error
+/* iters K-SVD iterations of every problem (each N >= 1): per iteration ONE persistent Batch-OMP
+ * launch over all problems (as ksvd_batched_omp), then every problem's dictionary update, error
  * and clearDict -- one after another with each sweep on the whole GPU, or (tuning
  * batch_concurrent) concurrently on their own streams with the cooperative sweeps sharing the
  * SMs in proportion to N*T.  D is normalised first and updated in place; idx/coef/nnz hold the last

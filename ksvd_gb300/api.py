@@ -366,7 +366,7 @@ class Handle:
         return arr, outs
 
     def batched_omp(self, problems, out=None):
-        """Batch-OMP of many independent problems in persistent launches (one per K class).
+        """Batch-OMP of many independent problems in one persistent launch.
 
         ``problems``: sequence of dicts with D (K, n) and X (N, n) float32 device tensors, T, and
         optional eps2 (N,) float32 (error targets).  Returns [(idx, coef, nnz), ...]."""

@@ -755,12 +755,11 @@ struct BatchPlan {
   int64_t tiles = 0;
   OmpJob* jdev = nullptr;
   int nj = 0;
+  int64_t chunks = 0;
+  int tmax = 1;
   int chunk = 1;
-  unsigned long long* queue = nullptr;   // one work-queue counter per class
+  unsigned long long* queue = nullptr;
   int* de = nullptr;
-  // jobs grouped by atom-padding class c (kpl = 4 << c), one Batch-OMP launch per class
-  int cls_first[4] = {}, cls_n[4] = {}, cls_tmax[4] = {};
-  int64_t cls_chunks[4] = {};
 };
 
 // Checks the problems, sizes the shared workspace and uploads the tables (asynchronously, from
@@ -769,6 +768,7 @@ struct BatchPlan {
 ksvd_status batched_omp_plan(ksvd_handle* h, const ksvd_problem* probs, int32_t nprob,
                              BatchPlan* pl) {
   int64_t g_off = 0, a_off = 0;
+  int tmax = 1;
   std::vector<int64_t> goff(nprob), aoff(nprob);
   for (int32_t i = 0; i < nprob; ++i) {
     const ksvd_problem& q = probs[i];
@@ -786,6 +786,7 @@ ksvd_status batched_omp_plan(ksvd_handle* h, const ksvd_problem* probs, int32_t 
     aoff[i] = a_off;
     g_off += round_up((int64_t)kp * kp, 64);
     a_off += round_up((int64_t)kp * q.N, 64);
+    tmax = std::max(tmax, (int)q.T);
   }
   float *Gall = nullptr, *Aall = nullptr;
   GemmDesc* ddev = nullptr;
@@ -796,45 +797,30 @@ ksvd_status batched_omp_plan(ksvd_handle* h, const ksvd_problem* probs, int32_t 
   KSVD_TRY(ensure(h, B_BA0, (size_t)a_off, &Aall));
   KSVD_TRY(ensure(h, B_BDESC, (size_t)2 * nprob, &ddev));
   KSVD_TRY(ensure(h, B_BJOB, (size_t)nprob, &jdev));
-  KSVD_TRY(ensure(h, B_BQUEUE, 4, &queue));
+  KSVD_TRY(ensure(h, B_BQUEUE, 1, &queue));
   KSVD_TRY(ensure(h, B_DEVERR, 1, &de));
   auto& descs = h->batch_descs;
   auto& jobs = h->batch_jobs;
   descs.assign(2 * (size_t)nprob, GemmDesc{});
   jobs.assign((size_t)nprob, OmpJob{});
-  int64_t tiles = 0;
+  int64_t tiles = 0, chunks = 0;
   int nd = 0, nj = 0;
   const int chunk = h->batch_chunk > 0 ? h->batch_chunk : omp_batch_chunk();
-  BatchPlan plan;
   for (int32_t i = 0; i < nprob; ++i) {
     const ksvd_problem& q = probs[i];
     if (q.N == 0) continue;
     const int kp = omp_padded_k(q.K);
-    tiles = gemm_desc_fill(descs[nd++], q.D, q.n, q.D, q.n, Gall + goff[i], kp, q.K, kp, q.K, kp,
-                           q.n, tiles);
-    tiles = gemm_desc_fill(descs[nd++], q.D, q.n, q.X, q.n, Aall + aoff[i], kp, q.K, kp, q.N, q.N,
-                           q.n, tiles);
+    float* G = Gall + goff[i];
+    float* A0 = Aall + aoff[i];
+    tiles = gemm_desc_fill(descs[nd++], q.D, q.n, q.D, q.n, G, kp, q.K, kp, q.K, kp, q.n, tiles);
+    tiles = gemm_desc_fill(descs[nd++], q.D, q.n, q.X, q.n, A0, kp, q.K, kp, q.N, q.N, q.n, tiles);
+    OmpJob& j = jobs[nj++];
+    j.G = G; j.ldg = kp; j.A0 = A0; j.lda = kp; j.X = q.X; j.ldx = q.n; j.eps2 = q.eps2;
+    j.idx = q.idx; j.coef = q.coef; j.nnz = q.nnz; j.N = q.N; j.chunk_begin = chunks;
+    j.n = q.n; j.K = q.K; j.kpl = kp / 32; j.T = q.T;
+    chunks += (q.N + chunk - 1) / chunk;
   }
-  for (int c = 0; c < 4; ++c) {
-    plan.cls_first[c] = nj;
-    for (int32_t i = 0; i < nprob; ++i) {
-      const ksvd_problem& q = probs[i];
-      const int kp = omp_padded_k(q.K);
-      if (q.N == 0 || kp / 32 != (4 << c)) continue;
-      OmpJob& j = jobs[nj++];
-      j.G = Gall + goff[i]; j.ldg = kp; j.A0 = Aall + aoff[i]; j.lda = kp;
-      j.X = q.X; j.ldx = q.n; j.eps2 = q.eps2;
-      j.idx = q.idx; j.coef = q.coef; j.nnz = q.nnz; j.N = q.N;
-      j.chunk_begin = plan.cls_chunks[c];
-      j.n = q.n; j.K = q.K; j.kpl = kp / 32; j.T = q.T;
-      plan.cls_chunks[c] += (q.N + chunk - 1) / chunk;
-      plan.cls_tmax[c] = std::max(plan.cls_tmax[c], (int)q.T);
-    }
-    plan.cls_n[c] = nj - plan.cls_first[c];
-  }
-  plan.ddev = ddev; plan.nd = nd; plan.tiles = tiles; plan.jdev = jdev; plan.nj = nj;
-  plan.chunk = chunk; plan.queue = queue; plan.de = de;
-  *pl = plan;
+  *pl = BatchPlan{ddev, nd, tiles, jdev, nj, chunks, tmax, chunk, queue, de};
   if (nj == 0) return KSVD_OK;
   // the host tables live in the handle, so the asynchronous copies read valid memory
   KSVD_CK(h, cudaMemcpyAsync(ddev, descs.data(), sizeof(GemmDesc) * nd, cudaMemcpyHostToDevice,
@@ -852,11 +838,8 @@ ksvd_status batched_omp_launch(ksvd_handle* h, const BatchPlan& pl) {
     KSVD_CK(h, launch_gemm_tn_f32_grouped(pl.ddev, pl.nd, pl.tiles, h->stream));
   }
   StageScope sc(h, KSVD_STAGE_OMP);
-  for (int c = 0; c < 4; ++c)
-    if (pl.cls_n[c] > 0)
-      KSVD_CK(h, launch_omp_batched(pl.jdev + pl.cls_first[c], pl.cls_n[c], pl.cls_chunks[c],
-                                    pl.cls_tmax[c], 4 << c, pl.chunk, pl.queue + c, pl.de,
-                                    h->stream));
+  KSVD_CK(h, launch_omp_batched(pl.jdev, pl.nj, pl.chunks, pl.tmax, pl.chunk, pl.queue, pl.de,
+                                h->stream));
   return KSVD_OK;
 }
 

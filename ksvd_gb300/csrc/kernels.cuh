@@ -158,10 +158,10 @@ struct OmpJob {
   int n, K, kpl, T;                 // kpl = Kp / 32 (4, 8, 16 or 32)
 };
 int omp_batch_chunk();              // default signals per work-queue chunk
-// jobs_dev sorted by chunk_begin (chunk_begin in units of `chunk` signals), every job of the
-// same kpl; tmax = max T over the jobs.  Zeroes *queue on the stream.
+// jobs_dev sorted by chunk_begin (chunk_begin in units of `chunk` signals); tmax = max T over
+// the jobs.  Zeroes *queue on the stream.
 cudaError_t launch_omp_batched(const OmpJob* jobs_dev, int njobs, int64_t total_chunks, int tmax,
-                               int kpl, int chunk, unsigned long long* queue, int* dev_err,
+                               int chunk, unsigned long long* queue, int* dev_err,
                                cudaStream_t st);
 
 // ---- grouped FP32 GEMM: many C = A'B products (different sizes) in one launch -------------------

@@ -508,18 +508,16 @@ omp_kernel(const float* __restrict__ G, const uint16_t* __restrict__ Gh,
 // comes from X in the same pass.
 constexpr int kBatchChunk = 16;   // default signals per work-queue chunk
 
-// One launch per atom-padding class (KPL = Kp / 32): each class's kernel has the registers and
-// the occupancy of its own alpha width instead of the widest class's.
-template <int TMAX, int KPL>
-__global__ void __launch_bounds__(kOmpWarps * 32, (KPL <= 8 ? 3 : 2))
+template <int TMAX>
+__global__ void __launch_bounds__(kOmpWarps * 32, 2)
 omp_batched_kernel(const OmpJob* __restrict__ jobs, int njobs, int64_t total_chunks,
                    int chunk, unsigned long long* __restrict__ queue, int* __restrict__ dev_err) {
   extern __shared__ __align__(16) float smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  float* L = smem + (size_t)wib * warp_smem_floats<KPL, TMAX>();
+  float* L = smem + (size_t)wib * warp_smem_floats<32, TMAX>();
   float* a0s = L + l_floats<TMAX>();
-  int* cand = reinterpret_cast<int*>(a0s + 32 * KPL);
+  int* cand = reinterpret_cast<int*>(a0s + 32 * 32);
   bool numeric_bad = false;
   for (;;) {
     unsigned long long c = 0;
@@ -546,8 +544,16 @@ omp_batched_kernel(const OmpJob* __restrict__ jobs, int njobs, int64_t total_chu
       const float* a0 = jb.A0 + s * jb.lda;
       int32_t* io = jb.idx + s * jb.T;
       float* co = jb.coef + s * jb.T;
-      omp_signal<KPL, TMAX, false>(jb.G, nullptr, 0.f, jb.ldg, a0, jb.K, jb.T, emode, e2, xn2, io,
-                                   co, jb.nnz + s, L, a0s, cand, numeric_bad);
+      switch (jb.kpl) {
+#define KSVD_BATCHED_SIGNAL(KPL)                                                              \
+  omp_signal<KPL, TMAX, false>(jb.G, nullptr, 0.f, jb.ldg, a0, jb.K, jb.T, emode, e2, xn2, io, \
+                               co, jb.nnz + s, L, a0s, cand, numeric_bad)
+        case 4: KSVD_BATCHED_SIGNAL(4); break;
+        case 8: KSVD_BATCHED_SIGNAL(8); break;
+        case 16: KSVD_BATCHED_SIGNAL(16); break;
+        default: KSVD_BATCHED_SIGNAL(32); break;
+#undef KSVD_BATCHED_SIGNAL
+      }
     }
   }
   if (__any_sync(KSVD_FULL_MASK, numeric_bad) && lane == 0) atomicOr(dev_err, kDevErrNumeric);
@@ -576,11 +582,11 @@ cudaError_t launch_omp_t(const float* G, const uint16_t* Gh, const unsigned* mu,
   return cudaGetLastError();
 }
 
-template <int TMAX, int KPL>
+template <int TMAX>
 cudaError_t launch_omp_batched_t(const OmpJob* jobs, int njobs, int64_t total_chunks, int chunk,
                                  unsigned long long* queue, int* dev_err, cudaStream_t st) {
-  const size_t smem = (size_t)kOmpWarps * warp_smem_floats<KPL, TMAX>() * sizeof(float);
-  auto kern = omp_batched_kernel<TMAX, KPL>;
+  const size_t smem = (size_t)kOmpWarps * warp_smem_floats<32, TMAX>() * sizeof(float);
+  auto kern = omp_batched_kernel<TMAX>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return e;
@@ -604,23 +610,13 @@ cudaError_t launch_omp_batched_t(const OmpJob* jobs, int njobs, int64_t total_ch
 int omp_batch_chunk() { return kBatchChunk; }
 
 cudaError_t launch_omp_batched(const OmpJob* jobs_dev, int njobs, int64_t total_chunks, int tmax,
-                               int kpl, int chunk, unsigned long long* queue, int* dev_err,
+                               int chunk, unsigned long long* queue, int* dev_err,
                                cudaStream_t st) {
   if (njobs <= 0 || total_chunks <= 0) return cudaSuccess;
   if (tmax < 1 || tmax > kMaxT || chunk < 1) return cudaErrorInvalidValue;
-#define KSVD_BATCHED_ARGS jobs_dev, njobs, total_chunks, chunk, queue, dev_err, st
-#define KSVD_BATCHED_KPL(TM)                                                    \
-  switch (kpl) {                                                                \
-    case 4: return launch_omp_batched_t<TM, 4>(KSVD_BATCHED_ARGS);              \
-    case 8: return launch_omp_batched_t<TM, 8>(KSVD_BATCHED_ARGS);              \
-    case 16: return launch_omp_batched_t<TM, 16>(KSVD_BATCHED_ARGS);            \
-    case 32: return launch_omp_batched_t<TM, 32>(KSVD_BATCHED_ARGS);            \
-    default: return cudaErrorInvalidValue;                                      \
-  }
-  if (tmax <= 32) { KSVD_BATCHED_KPL(32) }
-  KSVD_BATCHED_KPL(64)
-#undef KSVD_BATCHED_KPL
-#undef KSVD_BATCHED_ARGS
+  if (tmax <= 32)
+    return launch_omp_batched_t<32>(jobs_dev, njobs, total_chunks, chunk, queue, dev_err, st);
+  return launch_omp_batched_t<64>(jobs_dev, njobs, total_chunks, chunk, queue, dev_err, st);
 }
 
 int omp_padded_k(int K) {
