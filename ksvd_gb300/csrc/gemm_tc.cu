@@ -45,6 +45,10 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
                : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   for (uint32_t it = 0; it < kWaitLimit; ++it) {
     uint32_t done;
@@ -241,6 +245,184 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_constant
   }
 }
 
+// Persistent variant for many tiles: one CTA per SM walks tiles t = blockIdx.x, +gridDim.x, ...
+// (atom tile fastest).  Warp 0 lane 0 streams the inner chunks through a 4-stage TMA ring,
+// warp 1 lane 0 issues the MMAs into one of two 256-column TMEM accumulators, and warps 2-5
+// drain the other accumulator (each warp the TMEM lane quarter warp % 4 allows it): the
+// epilogue of tile t overlaps the MMAs of tile t+1.  Accumulator hand-off: tmem_full[b] (MMA
+// commit -> epilogue) and tmem_empty[b] (one arrival per epilogue warp -> MMA).  Every wait is
+// bounded; on a timeout the CTA records kDevErrTimeout, the roles stop and TMEM is freed.
+constexpr int PSTAGES = 4;
+constexpr int P_SMEM_BYTES = PSTAGES * STAGE_BYTES + 1024 + 256;
+constexpr uint32_t kTmemColsP = 2 * TN;
+constexpr int kEpiWarps = 4;
+
+__global__ void __launch_bounds__(192, 1)
+gemm_tc_persistent_kernel(const __grid_constant__ CUtensorMap tmA_hi,
+                          const __grid_constant__ CUtensorMap tmA_lo,
+                          const __grid_constant__ CUtensorMap tmB_hi,
+                          const __grid_constant__ CUtensorMap tmB_lo, TcParams P,
+                          int64_t ntiles) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + PSTAGES * STAGE_BYTES);
+  uint64_t* empty = full + PSTAGES;
+  uint64_t* tfull = empty + PSTAGES;
+  uint64_t* tempty = tfull + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + 2);
+  int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < PSTAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], kEpiWarps);
+    }
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(kTmemColsP)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  const int items = P.nk * P.passes;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- TMA producer: one global item counter across the CTA's tiles
+      int64_t g = 0;
+      bool ok = true;
+      for (int64_t t = blockIdx.x; ok && t < ntiles; t += gridDim.x) {
+        const int m0 = (int)(t % P.mtiles) * TM;
+        const int n0 = (int)((t / P.mtiles) * TN);
+        for (int it = 0; it < items; ++it, ++g) {
+          const int s = (int)(g % PSTAGES);
+          const uint32_t use = (uint32_t)(g / PSTAGES);
+          if ((g >= PSTAGES && !mbar_wait(&empty[s], (use - 1) & 1)) ||
+              *(volatile int*)abort_flag) {
+            if (!*(volatile int*)abort_flag) atomicOr(P.dev_err, kDevErrTimeout);
+            *(volatile int*)abort_flag = 1;
+            ok = false;
+            break;
+          }
+          const int pass = it / P.nk, kc = it % P.nk;
+          const CUtensorMap* ta = pass == 2 ? &tmA_lo : &tmA_hi;
+          const CUtensorMap* tb = pass == 1 ? &tmB_lo : &tmB_hi;
+          uint8_t* sa = smem + s * STAGE_BYTES;
+          uint8_t* sb = sa + A_BYTES;
+          mbar_expect_tx(&full[s], STAGE_BYTES);
+          tma_load_2d(ta, &full[s], sa, kc * TK, m0);
+          tma_load_2d(tb, &full[s], sb, kc * TK, n0);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer: tile lt of this CTA accumulates into buffer lt & 1
+      int64_t g = 0;
+      bool ok = true;
+      int lt = 0;
+      for (int64_t t = blockIdx.x; ok && t < ntiles; t += gridDim.x, ++lt) {
+        const int b = lt & 1;
+        const uint32_t tuse = (uint32_t)(lt >> 1);
+        if (lt >= 2 && !mbar_wait(&tempty[b], (tuse - 1) & 1)) {
+          atomicOr(P.dev_err, kDevErrTimeout);
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t tacc = tmem + (uint32_t)(b * TN);
+        for (int it = 0; it < items; ++it, ++g) {
+          const int s = (int)(g % PSTAGES);
+          const uint32_t use = (uint32_t)(g / PSTAGES);
+          if (!mbar_wait(&full[s], use & 1) || *(volatile int*)abort_flag) {
+            if (!*(volatile int*)abort_flag) atomicOr(P.dev_err, kDevErrTimeout);
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t sa = smem_u32(smem + s * STAGE_BYTES);
+          const uint32_t sb = sa + A_BYTES;
+          const uint64_t ad = sw128_desc(sa), bd = sw128_desc(sb);
+#pragma unroll
+          for (int j = 0; j < TK / 16; ++j)
+            umma_bf16(tacc, ad + 2 * j, bd + 2 * j, (it > 0 || j > 0) ? 1u : 0u);
+          umma_commit(&empty[s]);
+        }
+        if (ok) umma_commit(&tfull[b]);
+      }
+      if (!ok) *(volatile int*)abort_flag = 1;
+    }
+  } else {
+    // ---- epilogue warps 2..5: TMEM lanes (atoms m0 + 32 * (warp % 4) + lane)
+    const int q = warp & 3;
+    int lt = 0;
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
+      const int b = lt & 1;
+      const uint32_t tuse = (uint32_t)(lt >> 1);
+      const int m0 = (int)(t % P.mtiles) * TM;
+      const int64_t n0 = (t / P.mtiles) * TN;
+      bool have = mbar_wait(&tfull[b], tuse & 1);
+      have = __all_sync(KSVD_FULL_MASK, have && *(volatile int*)abort_flag == 0);
+      if (!have) {
+        if (lane == 0) atomicOr(P.dev_err, kDevErrTimeout);
+        *(volatile int*)abort_flag = 1;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int row = m0 + q * 32 + lane;
+      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * TN);
+#pragma unroll 1
+      for (int c0 = 0; c0 < TN; c0 += 32) {
+        uint32_t v[32];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+            "%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+              "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+              "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]),
+              "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
+              "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]),
+              "=r"(v[31])
+            : "r"(taddr + (uint32_t)c0));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (row < P.M) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int64_t s = n0 + c0 + j;
+            if (s < P.Ncols) __stcs(P.C + s * P.ldc + row, __uint_as_float(v[j]));
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty[b]);   // this warp is done with the accumulator
+    }
+  }
+  __syncwarp();                        // warps 0 and 1: lane 0 rejoins the others
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(kTmemColsP)
+                 : "memory");
+  }
+}
+
 __global__ void split_bf16_kernel(const float* __restrict__ in, int64_t ld_in, int64_t rows,
                                   int inner, __nv_bfloat16* __restrict__ hi,
                                   __nv_bfloat16* __restrict__ lo, int64_t ld_out,
@@ -331,9 +513,6 @@ cudaError_t launch_gemm_tn_bf16(const TcOperand& A, const TcOperand& B, float* C
     ma_lo = ma_hi;
     mb_lo = mb_hi;
   }
-  cudaError_t e = cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       SMEM_BYTES);
-  if (e != cudaSuccess) return e;
   TcParams P;
   P.C = C;
   P.ldc = ldc;
@@ -346,7 +525,24 @@ cudaError_t launch_gemm_tn_bf16(const TcOperand& A, const TcOperand& B, float* C
   const int gy = (M + TM - 1) / TM;
   if (gx * gy > 0x7fffffffLL) return cudaErrorInvalidValue;
   P.mtiles = gy;
-  gemm_tc_kernel<<<(unsigned)(gx * gy), 128, SMEM_BYTES, st>>>(ma_hi, ma_lo, mb_hi, mb_lo, P);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t ntiles = gx * gy;
+  cudaError_t e;
+  if (ntiles > sms) {
+    // many tiles: persistent CTAs, the epilogue of one tile under the MMAs of the next
+    e = cudaFuncSetAttribute(gemm_tc_persistent_kernel,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, P_SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    gemm_tc_persistent_kernel<<<(unsigned)sms, 192, P_SMEM_BYTES, st>>>(ma_hi, ma_lo, mb_hi,
+                                                                          mb_lo, P, ntiles);
+    return cudaGetLastError();
+  }
+  e = cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           SMEM_BYTES);
+  if (e != cudaSuccess) return e;
+  gemm_tc_kernel<<<(unsigned)ntiles, 128, SMEM_BYTES, st>>>(ma_hi, ma_lo, mb_hi, mb_lo, P);
   return cudaGetLastError();
 }
 
