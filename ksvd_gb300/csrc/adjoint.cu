@@ -10,8 +10,8 @@
 // so dL/dD(:, S_t) += r u_t - (A u) gamma_t  (accumulated with float atomics: the order of the
 // additions, and so the last bits of dL/dD, vary from run to run).
 // One warp per signal; the signal and the reconstruction live in registers (n/32 per lane), the
-// factor in shared memory.  The reference has no differentiable path; the benchmark spec asks for
-// one (gradients w.r.t. D and X through the coding step, checked against FP64 differences).
+// factor in shared memory.  The reference has no differentiable path; this one gives the
+// gradients w.r.t. D and X through the coding step (checked against FP64 finite differences).
 #include "common.cuh"
 #include "kernels.cuh"
 
