@@ -224,7 +224,8 @@ KSVD_API int64_t ksvd_graph_replays(const ksvd_handle* handle);
 
 /* Launch shapes chosen per handle (0 = the built-in default). */
 typedef struct ksvd_tuning {
-  int32_t omp_grid_mult; /* Batch-OMP blocks = resident CTA slots x this (grid-stride)          */
+  int32_t omp_grid_mult; /* Batch-OMP blocks = resident CTA slots x this (grid-stride); 0 (the
+                            default): one resident grid, warps claim signals from a queue      */
   int32_t sweep_ctas;    /* CTAs of the cooperative atom sweep (0: one per SM)                  */
   int32_t batch_chunk;   /* signals per work-queue chunk of the batched Batch-OMP (default 16)  */
   int32_t batch_concurrent; /* ksvd_batched_iterate: 1 = per-problem updates concurrently on

@@ -101,7 +101,7 @@ enum BufId {
   B_DPAD, B_G, B_A0, B_XN2, B_LIST, B_START, B_BHIST, B_Y, B_GN2, B_C, B_AVEC, B_AD, B_PART,
   B_UNUSED, B_BITMAP, B_REPLACED, B_COUNTER, B_USE, B_BARRIER, B_ERR, B_PSUM, B_BVAL, B_BIDX,
   B_RMSE, B_M, B_MI, B_CLEARED, B_DEVERR, B_PERM, B_GPAD_IN, B_HX, B_HD, B_HIDX, B_HCOEF, B_HNNZ,
-  B_XHI, B_XLO, B_DHI, B_DLO, B_P, B_BG, B_BA0, B_BDESC, B_BJOB, B_BQUEUE, B_ITER, B_RPART, B_RMEAN, B_TUNE_D, B_TUNE_C, B_GH, B_MU, B_COUNT
+  B_XHI, B_XLO, B_DHI, B_DLO, B_P, B_BG, B_BA0, B_BDESC, B_BJOB, B_BQUEUE, B_ITER, B_RPART, B_RMEAN, B_TUNE_D, B_TUNE_C, B_GH, B_MU, B_OMPQ, B_COUNT
 };
 
 ksvd_status fail(ksvd_handle* h, ksvd_status s, const char* fmt, const char* detail = nullptr) {
@@ -352,10 +352,12 @@ ksvd_status run_omp(ksvd_handle* h, const float* G, const float* A0, int64_t N,
     KSVD_TRY(ensure(h, B_GH, (size_t)h->Kp * h->Kp, &gh));
     KSVD_TRY(ensure(h, B_MU, 1, &mu));
   }
+  unsigned long long* q = nullptr;     // grid_mult 0: signals claimed from a work queue
+  if (h->omp_grid_mult == 0) KSVD_TRY(ensure(h, B_OMPQ, 1, &q));
   StageScope sc(h, KSVD_STAGE_OMP);
   if (gh) KSVD_CK(h, launch_gram_half(G, h->Kp, h->p.K, gh, mu, h->stream));
   KSVD_CK(h, launch_omp(G, h->Kp, A0, h->Kp, h->p.K, N, h->p.T, xnorm2, eps2, idx, coef, nnz, de,
-                        h->stream, h->omp_grid_mult, gh, mu));
+                        h->stream, h->omp_grid_mult, gh, mu, q));
   return KSVD_OK;
 }
 
@@ -988,7 +990,7 @@ ksvd_status ksvd_autotune(ksvd_handle* h, const float* D, const float* X, int64_
   for (int fp16 : {0, 1}) {
     if (!try_fp16 && fp16 == 1) break;
     if (try_fp16) h->omp_fp16 = fp16;
-    for (int mult : {1, 2, 4, 8, 16}) {
+    for (int mult : {0, 1, 2, 4, 8, 16}) {
       h->omp_grid_mult = mult;
       double ms = 0;
       st = time_on_stream(h, 3, [&] {

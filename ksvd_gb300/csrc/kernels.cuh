@@ -38,14 +38,16 @@ cudaError_t launch_split_bf16(const float* in, int64_t ld_in, int64_t rows, int 
 int omp_padded_k(int K);
 // G: Kp x Kp column-major (ldg >= Kp), zero padded; A0: Kp x N column-major (lda >= Kp), zero
 // padded, with Kp = omp_padded_k(K).  T <= 64.
-// grid_mult: resident CTAs per SM x grid_mult blocks at most (0 = default 8; the autotuner's knob)
+// grid_mult: resident CTAs per SM x grid_mult blocks at most, signals assigned grid-stride; 0 with
+// a queue (one zeroed counter): one resident grid whose warps claim signals from the queue (0
+// without a queue: 8; the autotuner's knob)
 // Gh/mu (mixed path, T <= 32): FP16 copy of G and its coherence from launch_gram_half; the alpha
 // update then reads Gh and resolves near ties in FP32 (the selection is the FP32 Batch-OMP's).
 cudaError_t launch_omp(const float* G, int64_t ldg, const float* A0, int64_t lda, int K,
                        int64_t N, int T, const float* xnorm2, const float* eps2, int32_t* idx,
                        float* coef, int32_t* nnz, int* dev_err, cudaStream_t st,
                        int grid_mult = 0, const uint16_t* Gh = nullptr,
-                       const unsigned* mu = nullptr);
+                       const unsigned* mu = nullptr, unsigned long long* queue = nullptr);
 // Gh = FP16(G) (Kp x Kp, same ldg) and mu = max off-diagonal |G(i, j)|, i, j < K.
 cudaError_t launch_gram_half(const float* G, int64_t ldg, int K, uint16_t* Gh, unsigned* mu,
                              cudaStream_t st);

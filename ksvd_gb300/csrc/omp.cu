@@ -25,6 +25,7 @@ namespace ksvd {
 namespace {
 
 constexpr int kOmpWarps = 8;
+constexpr int kOmpClaim = 4;   // signals per work-queue claim of the single-problem kernel
 
 // Shared-memory layout of the Cholesky factor L (TMAX x TMAX, lower): rows of stride TMAX+1
 // (bank-conflict padding) up to TMAX = 32; for TMAX = 64 packed by rows (row r at r(r+1)/2),
@@ -477,13 +478,14 @@ __device__ __forceinline__ float h16_tolerance(const unsigned* mu_bits) {
   return ldexpf(__uint_as_float(*mu_bits), -12) + ldexpf(1.f, -18);
 }
 
-template <int KPL, int TMAX, bool H16>
+template <int KPL, int TMAX, bool H16, bool QUEUE>
 __global__ void __launch_bounds__(kOmpWarps * 32, (TMAX <= 32 ? 3 : 2))
 omp_kernel(const float* __restrict__ G, const uint16_t* __restrict__ Gh,
            const unsigned* __restrict__ mu_bits, int64_t ldg, const float* __restrict__ A0,
            int64_t lda, int K, int64_t N, int T, const float* __restrict__ xnorm2,
            const float* __restrict__ eps2, int32_t* __restrict__ idx_out,
-           float* __restrict__ coef_out, int32_t* __restrict__ nnz_out, int* __restrict__ dev_err) {
+           float* __restrict__ coef_out, int32_t* __restrict__ nnz_out, int* __restrict__ dev_err,
+           unsigned long long* __restrict__ queue) {
   extern __shared__ __align__(16) float smem[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
@@ -491,13 +493,31 @@ omp_kernel(const float* __restrict__ G, const uint16_t* __restrict__ Gh,
   float* a0s = L + l_floats_for<TMAX>(T);                                // alpha0 column
   int* cand = reinterpret_cast<int*>(a0s + 32 * KPL);
   const float tol = H16 ? h16_tolerance(mu_bits) : 0.f;
-  const int64_t warps_total = (int64_t)gridDim.x * kOmpWarps;
   bool numeric_bad = false;
   const bool emode = eps2 != nullptr;
-  for (int64_t s = (int64_t)blockIdx.x * kOmpWarps + wib; s < N; s += warps_total)
-    omp_signal<KPL, TMAX, H16>(G, Gh, tol, ldg, A0 + s * lda, K, T, emode,
-                               emode ? eps2[s] : 0.f, emode ? xnorm2[s] : 0.f, idx_out + s * T,
-                               coef_out + s * T, nnz_out + s, L, a0s, cand, numeric_bad);
+  if constexpr (QUEUE) {
+    // resident grid: warps claim kOmpClaim signals at a time from *queue (zeroed before the
+    // launch); early stops make signals uneven, and the last claims even the SMs out
+    for (;;) {
+      unsigned long long cl = 0;
+      if (lane == 0) cl = atomicAdd(queue, 1ull);
+      cl = __shfl_sync(KSVD_FULL_MASK, cl, 0);
+      const int64_t s0 = (int64_t)cl * kOmpClaim;
+      if (s0 >= N) break;
+      const int64_t s1 = min(N, s0 + kOmpClaim);
+      for (int64_t s = s0; s < s1; ++s)
+        omp_signal<KPL, TMAX, H16>(G, Gh, tol, ldg, A0 + s * lda, K, T, emode,
+                                   emode ? eps2[s] : 0.f, emode ? xnorm2[s] : 0.f,
+                                   idx_out + s * T, coef_out + s * T, nnz_out + s, L, a0s, cand,
+                                   numeric_bad);
+    }
+  } else {
+    const int64_t warps_total = (int64_t)gridDim.x * kOmpWarps;
+    for (int64_t s = (int64_t)blockIdx.x * kOmpWarps + wib; s < N; s += warps_total)
+      omp_signal<KPL, TMAX, H16>(G, Gh, tol, ldg, A0 + s * lda, K, T, emode,
+                                 emode ? eps2[s] : 0.f, emode ? xnorm2[s] : 0.f, idx_out + s * T,
+                                 coef_out + s * T, nnz_out + s, L, a0s, cand, numeric_bad);
+  }
   if (__any_sync(KSVD_FULL_MASK, numeric_bad) && lane == 0) atomicOr(dev_err, kDevErrNumeric);
 }
 
@@ -563,9 +583,12 @@ template <int KPL, int TMAX, bool H16>
 cudaError_t launch_omp_t(const float* G, const uint16_t* Gh, const unsigned* mu, int64_t ldg,
                          const float* A0, int64_t lda, int K, int64_t N, int T,
                          const float* xnorm2, const float* eps2, int32_t* idx, float* coef,
-                         int32_t* nnz, int* dev_err, int grid_mult, cudaStream_t st) {
+                         int32_t* nnz, int* dev_err, int grid_mult, unsigned long long* queue,
+                         cudaStream_t st) {
   const size_t smem = (size_t)kOmpWarps * warp_smem_floats_for<KPL, TMAX>(T) * sizeof(float);
-  auto kern = omp_kernel<KPL, TMAX, H16>;
+  // grid_mult 0 with a queue: one resident grid, signals claimed from the queue
+  const bool use_queue = queue != nullptr && grid_mult == 0;
+  auto kern = use_queue ? omp_kernel<KPL, TMAX, H16, true> : omp_kernel<KPL, TMAX, H16, false>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return e;
@@ -575,10 +598,15 @@ cudaError_t launch_omp_t(const float* G, const uint16_t* Gh, const unsigned* mu,
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kOmpWarps * 32, smem);
   if (per_sm < 1) per_sm = 1;
   int64_t blocks = (N + kOmpWarps - 1) / kOmpWarps;
-  const int64_t cap = (int64_t)sms * per_sm * (grid_mult > 0 ? grid_mult : 8);
+  const int64_t cap = (int64_t)sms * per_sm * (use_queue ? 1 : (grid_mult > 0 ? grid_mult : 8));
   if (blocks > cap) blocks = cap;
+  if (use_queue) {
+    e = cudaMemsetAsync(queue, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+  }
   kern<<<(unsigned)blocks, kOmpWarps * 32, smem, st>>>(G, Gh, mu, ldg, A0, lda, K, N, T, xnorm2,
-                                                       eps2, idx, coef, nnz, dev_err);
+                                                       eps2, idx, coef, nnz, dev_err,
+                                                       use_queue ? queue : nullptr);
   return cudaGetLastError();
 }
 
@@ -658,7 +686,7 @@ cudaError_t launch_gram_half(const float* G, int64_t ldg, int K, uint16_t* Gh, u
 cudaError_t launch_omp(const float* G, int64_t ldg, const float* A0, int64_t lda, int K,
                        int64_t N, int T, const float* xnorm2, const float* eps2, int32_t* idx,
                        float* coef, int32_t* nnz, int* dev_err, cudaStream_t st, int grid_mult,
-                       const uint16_t* Gh, const unsigned* mu) {
+                       const uint16_t* Gh, const unsigned* mu, unsigned long long* queue) {
   if (N <= 0) return cudaSuccess;
   if (K < 1 || K > kMaxK || T < 1 || T > kMaxT) return cudaErrorInvalidValue;
   const int kp = omp_padded_k(K);   // the lanes touch rows [0, kp) of every column
@@ -666,7 +694,7 @@ cudaError_t launch_omp(const float* G, int64_t ldg, const float* A0, int64_t lda
   if ((Gh == nullptr) != (mu == nullptr)) return cudaErrorInvalidValue;
   if (Gh && (ldg & 7)) return cudaErrorInvalidValue;   // 16-byte rows of eight FP16 values
 #define KSVD_OMP_ARGS G, Gh, mu, ldg, A0, lda, K, N, T, xnorm2, eps2, idx, coef, nnz, dev_err, \
-                      grid_mult, st
+                      grid_mult, queue, st
   if (T <= 32 && Gh) {
     switch (kp) {
       case 128: return launch_omp_t<4, 32, true>(KSVD_OMP_ARGS);
