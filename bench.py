@@ -135,13 +135,13 @@ def stage_flops(cfg, N, stage):
 # in proportion to the signals, so the bench scales it to its N.  profiles/omp_kernel_cfg2.md.
 # Keyed by (stage, n, K, T, precision): the mixed path runs the FP16-update Batch-OMP kernel.
 MEASURED_TRAFFIC = {("omp", 256, 1024, 16, "fp32"): (414.167808e6 + 7.126272e6) / 100_000,
-                    ("omp", 256, 1024, 16, "mixed"): (416.039680e6 + 7.574528e6) / 100_000}
+                    ("omp", 256, 1024, 16, "mixed"): (415.977472e6 + 7.665152e6) / 100_000}
 
 # Batch-OMP re-reads G's support columns from L2 every step: L2 throughput in percent of peak
 # (lts__throughput.avg.pct_of_peak_sustained_elapsed) and issue-active percent from the same
 # captures -- the FP32 kernel is bound by L2, the FP16-update kernel by instruction issue.
 MEASURED_L2_PCT = {("omp", 256, 1024, 16, "fp32"): (77.16, 52.73),
-                   ("omp", 256, 1024, 16, "mixed"): (47.63, 67.88)}
+                   ("omp", 256, 1024, 16, "mixed"): (47.52, 67.75)}
 
 # FP32 CUDA-core peak (nominal): 152 SMs x 128 FMA lanes x 2 FLOP x 2.07 GHz.
 FP32_SIMT_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
