@@ -44,6 +44,36 @@ def test_header_compiles_as_c():
     assert r.returncode == 0, r.stderr
 
 
+def test_struct_layouts_match_bindings(tmp_path):
+    """The ctypes structures of the Python binding have the C header's layout: every field at
+    the same offset and the same total size, so a change to either side is caught here."""
+    import ctypes as C
+
+    from ksvd_gb300 import _native
+
+    structs = {"ksvd_params": _native.Params, "ksvd_tuning": _native.Tuning,
+               "ksvd_problem": _native.Problem, "ksvd_stage_times": _native.StageTimes}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "ksvd_gb300.h"',
+             'int main(void) {']
+    for cname, py in structs.items():
+        lines.append('printf("%s sizeof %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f, _ in py._fields_:
+            lines.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, f))
+    lines += ['return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-std=c99", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, py in structs.items():
+        assert got[(cname, "sizeof")] == C.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
+
+
 def test_status_strings_and_defaults(native_lib):
     from ksvd_gb300._native import Params
 
