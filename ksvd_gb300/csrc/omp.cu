@@ -247,10 +247,8 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
 #pragma unroll
             for (int g = 0; g < NG; ++g)
 #pragma unroll
-              for (int q = 0; q < V; ++q) {
-                const int k = 32 * V * g + V * lane + q;
+              for (int q = 0; q < V; ++q)
                 if (fabsf(al[g][q]) >= thr) mine |= 1u << (V * g + q);
-              }
             const int cnt = __popc(mine);
             int incl = cnt;
 #pragma unroll
