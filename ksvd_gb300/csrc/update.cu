@@ -305,9 +305,8 @@ __device__ __forceinline__ void prefetch_l2_lines(const void* p, uint32_t bytes)
   const uintptr_t a0 = reinterpret_cast<uintptr_t>(p) & ~uintptr_t(127);
   const uintptr_t a1 = reinterpret_cast<uintptr_t>(p) + bytes;
   for (uintptr_t a = a0; a < a1; a += 128) {
-    unsigned v;
-    asm volatile("ld.global.cg.b32 %0, [%1];" : "=r"(v) : "l"(a) : "memory");
-    (void)v;                           // the load itself is the point
+    // the load itself is the point: its result goes to a PTX-local register
+    asm volatile("{\n .reg .b32 t;\n ld.global.cg.b32 t, [%0];\n}" ::"l"(a) : "memory");
   }
 }
 
