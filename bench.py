@@ -130,18 +130,27 @@ def stage_flops(cfg, N, stage):
     return 0.0
 
 
-# DRAM bytes per signal of one launch, from ncu captures (dram__bytes_read.sum +
-# dram__bytes_write.sum) of the same kernel on 100,000 signals of the same (n, K, T); traffic grows
-# in proportion to the signals, so the bench scales it to its N.  profiles/omp_kernel_cfg2.md.
-# Keyed by (stage, n, K, T, precision): the mixed path runs the FP16-update Batch-OMP kernel.
-MEASURED_TRAFFIC = {("omp", 256, 1024, 16, "fp32"): (414.167808e6 + 7.126272e6) / 100_000,
-                    ("omp", 256, 1024, 16, "mixed"): (415.977472e6 + 7.665152e6) / 100_000}
+# DRAM bytes per signal of one launch from an ncu capture (dram__bytes_read.sum +
+# dram__bytes_write.sum) of the same kernel on 100,000 signals of the same (n, K, T) -- traffic
+# grows in proportion to the signals, so the bench scales it to its N -- with the capture's L2
+# throughput and issue activity (lts__throughput, smsp__issue_active, percent of peak).  Each
+# entry is keyed by the fingerprint of the kernel source it was measured on (KERNEL_SOURCES): when
+# the source changes, no entry matches and the line reports traffic as null instead of a stale
+# figure.
+KERNEL_SOURCES = {"omp": ("omp.cu",)}
+MEASURED_OMP = {}   # (n, K, T, precision, fingerprint) -> (bytes per signal, L2 %, issue %)
 
-# Batch-OMP re-reads G's support columns from L2 every step: L2 throughput in percent of peak
-# (lts__throughput.avg.pct_of_peak_sustained_elapsed) and issue-active percent from the same
-# captures -- the FP32 kernel is bound by L2, the FP16-update kernel by instruction issue.
-MEASURED_L2_PCT = {("omp", 256, 1024, 16, "fp32"): (77.16, 52.73),
-                   ("omp", 256, 1024, 16, "mixed"): (47.52, 67.75)}
+
+def source_fingerprint(stage):
+    """sha256 (16 hex digits) of the kernel sources of a stage."""
+    import hashlib
+
+    h = hashlib.sha256()
+    for f in KERNEL_SOURCES.get(stage, ()):
+        with open(os.path.join(ROOT, "ksvd_gb300", "csrc", f), "rb") as fh:
+            h.update(f.encode() + b"\0" + fh.read())
+    return h.hexdigest()[:16]
+
 
 # FP32 CUDA-core peak (nominal): 152 SMs x 128 FMA lanes x 2 FLOP x 2.07 GHz.
 FP32_SIMT_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
@@ -197,8 +206,10 @@ def run_reference(args, cfg):
     oracle.build()
     threads = oracle.num_threads()
     Ns = min(cfg.N, args.cpu_sample)
-    p = datagen.make_problem(cfg, N=Ns)
-    X, D = p["X"], p["D"]
+    Nl = min(cfg.N, 4 * Ns)                 # a second, larger sample: is the cost linear in N?
+    p = datagen.make_problem(cfg, N=Nl)
+    XL, DL = p["X"], p["D"]
+    X, D = np.asfortranarray(XL[:, :Ns]), DL.copy(order="F")
     rng = np.random.default_rng(0)
     times = []
     for step in range(args.warmup + args.steps):
@@ -210,6 +221,15 @@ def run_reference(args, cfg):
             times.append(dt)
     t = statistics.median(times)
     value = 1.0 / (t * cfg.N / Ns)          # iterations/s at the full N, linear in N
+    lin = None
+    if Nl > Ns:
+        perm = rng.permutation(cfg.K).astype(np.int32)[None, :]
+        t0 = time.perf_counter()
+        oracle.ksvd(XL, DL.copy(order="F"), cfg.T, 1, perm)
+        tl = time.perf_counter() - t0
+        lin = {"signals": [Ns, Nl], "s_per_signal": [t / Ns, tl / Nl],
+               "ratio_large_over_small": (tl / Nl) / (t / Ns),
+               "value_from_large_sample": 1.0 / (tl * cfg.N / Nl)}
     line = {
         "impl": "reference", "metric": "ksvd_iters_per_s", "value": value, "unit": "iter/s",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -219,8 +239,13 @@ def run_reference(args, cfg):
                    % (cfg.name, cfg.n, cfg.K, cfg.N, cfg.T), "n": cfg.n, "K": cfg.K,
                    "N": cfg.N, "T": cfg.T},
         "cpu_baseline": {"value": value, "unit": "iter/s", "cores": threads, "kind": "port",
-                         "sample": "%d of %d signals per step, median of %d steps, scaled by N"
-                         % (Ns, cfg.N, args.steps)},
+                         "sample": "%d of %d signals per step (%.2f s each), median of %d steps, "
+                         "scaled by N; linearity check: one iteration on %d signals costs %s the "
+                         "per-signal time of the %d-signal steps"
+                         % (Ns, cfg.N, t, args.steps, Nl,
+                            "%.3fx" % lin["ratio_large_over_small"] if lin else "(n/a)", Ns),
+                         "linearity": lin},
+        "sample_s_per_step": t,
         "e2e": {"value": value, "unit": "iter/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -240,18 +265,30 @@ def cpu_baseline(cfg, sample, reps=1, check_iters=3, check_signals=20000):
 
     oracle.build()
     Ns = min(cfg.N, sample)
-    p = datagen.make_problem(cfg, N=Ns)
+    Nl = min(cfg.N, 4 * Ns)                 # a second, larger sample: is the cost linear in N?
+    p = datagen.make_problem(cfg, N=Nl)
     perm = np.random.default_rng(0).permutation(cfg.K).astype(np.int32)[None, :]
+    Xs = np.asfortranarray(p["X"][:, :Ns])
     ts = []
     for _ in range(reps):
         t0 = time.perf_counter()
-        oracle.ksvd(p["X"], p["D"], cfg.T, 1, perm)
+        oracle.ksvd(Xs, p["D"], cfg.T, 1, perm)
         ts.append(time.perf_counter() - t0)
     t = statistics.median(ts)
+    tl = None
+    if Nl > Ns:
+        t0 = time.perf_counter()
+        oracle.ksvd(p["X"], p["D"], cfg.T, 1, perm)
+        tl = time.perf_counter() - t0
     base = {"value": 1.0 / (t * cfg.N / Ns), "unit": "iter/s", "cores": oracle.num_threads(),
             "kind": "port",
-            "sample": "one K-SVD iteration on %d of %d signals (%.2f s), scaled by N" %
-                      (Ns, cfg.N, t)}
+            "sample": "one K-SVD iteration on %d of %d signals (%.2f s), scaled by N%s" %
+                      (Ns, cfg.N, t, "" if tl is None else
+                       "; on %d signals %.2f s (%.3fx the per-signal time)"
+                       % (Nl, tl, (tl / Nl) / (t / Ns)))}
+    if tl is not None:
+        base["linearity"] = {"signals": [Ns, Nl], "s_per_signal": [t / Ns, tl / Nl],
+                             "ratio_large_over_small": (tl / Nl) / (t / Ns)}
     check = None
     if check_iters > 0:
         rng = np.random.default_rng(1)
@@ -331,7 +368,7 @@ def run_batched(args):
     if rank == 0 and ws == 1 and not args.no_cpu:
         cpu = cpu_baseline_batched(probs, max(200, args.cpu_sample // 64))
     Ntot = sum(q["N"] for q in probs)
-    h = Handle(1, 1, 1, profile=True)
+    h = Handle(1, 1, 1, profile=True, precision=args.precision)
     tuning = h.autotune_batched(probs)
     outs, _ = h.batched_iterate(probs, args.warmup)
     torch.cuda.synchronize()
@@ -384,15 +421,19 @@ def run_batched(args):
     line = {
         "metric": "ksvd_batched_iters_per_s", "value": args.steps / (ms / 1e3), "unit": "iter/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32" if args.precision == "fp32" else "bf16-mixed",
         "data": "synthetic (seeded, cfg3 shapes)",
         "config": {"workload": "cfg3: %d problems, n in {32,64,128,256}, K=4n, %d signals in all,"
                    " error-constrained OMP, one K-SVD iteration of every problem per step"
                    % (len(probs), Ntot), "problems": len(probs), "signals": Ntot,
+                   "precision": args.precision,
                    "l2": "inputs larger than L2 (X = %.2f GB)"
                    % (sum(q["X"].numel() for q in probs) * 4 / 1e9), "autotuned": tuning},
         "omp_signals_per_s": {"value": Ntot / ((omp_ms + gemm_ms) / 1e3), "unit": "signals/s",
-                              "stages": "grouped D'X/Gram GEMM + persistent batched OMP",
+                              "stages": "D'X/Gram GEMMs (grouped FP32, or per-problem "
+                                        "tensor-core products for the mixed path) + persistent "
+                                        "batched OMP",
                               "omp_ms": omp_ms, "gemm_ms": gemm_ms},
         "support_sizes": {"min": int(sizes.min()), "mean": float(sizes.mean()),
                           "max": int(sizes.max())},
@@ -524,7 +565,8 @@ def main():
     # CPU baseline first (before any CUDA work in this process), rank 0 at N=1 only
     cpu = check = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        cpu, check = cpu_baseline(cfg, args.cpu_sample)
+        # the FP64 check runs as many iterations as this run times (warm-up included)
+        cpu, check = cpu_baseline(cfg, args.cpu_sample, check_iters=args.warmup + args.steps)
 
     prob = datagen.make_problem(cfg, N=args.signals,
                                 seed=datagen.SEED_BASE + cfg.index + 1000 * rank, device="cuda")
@@ -583,6 +625,11 @@ def main():
                     "rmse_max_rel_diff": max(abs(a - b) / b for a, b in zip(rms, rf)),
                     "rmse_per_iter_mixed": rms, "rmse_per_iter_fp32": rf}
         hf.close()
+    if cpu is not None:
+        # like for like beside the headline: the FP32 GPU path against the FP32 CPU port
+        cpu["mixed_gpu_over_cpu"] = value / cpu["value"]
+        if fp32_leg is not None:
+            cpu["fp32_gpu_over_cpu"] = fp32_leg["value"] / cpu["value"]
     fp64_check = None
     if check is not None:
         fp64_check = error_vs_fp64(cfg, check, args.precision, dev)
@@ -604,24 +651,25 @@ def main():
         ach = stage_bytes(cfg, N, dom) / (launch_ms / 1e3) / 1e9
         roof = {"bound": "hbm", "achieved": ach, "peak": pk["hbm"], "unit": "GB/s",
                 "frac": ach / pk["hbm"], "traffic": None}
-    tpu = MEASURED_TRAFFIC.get((dom, cfg.n, cfg.K, cfg.T, args.precision))
-    if tpu is not None and roof["bound"] == "hbm":
-        roof["traffic"] = tpu * N
-        roof["traffic_source"] = "ncu capture at N=100000, scaled by N"
+    fp = source_fingerprint(dom) if dom in KERNEL_SOURCES else None
+    meas = MEASURED_OMP.get((cfg.n, cfg.K, cfg.T, args.precision, fp)) if dom == "omp" else None
+    if meas is not None and roof["bound"] == "hbm":
+        roof["traffic"] = meas[0] * N
+        roof["traffic_source"] = "ncu capture at N=100000 of this kernel source, scaled by N"
+    elif dom in KERNEL_SOURCES:
+        roof["traffic_source"] = ("no ncu capture of kernel source %s at this shape: not "
+                                  "reported" % fp)
     fl = stage_flops(cfg, N, dom)
     if dom == "omp" and fl > 0:
         # the OMP step's alpha updates also have a compute roof (FP32 CUDA cores)
         tf = fl / (launch_ms / 1e3) / 1e12
         roof["compute"] = {"achieved": tf, "peak": FP32_SIMT_TFLOPS, "unit": "TFLOP/s",
                            "frac": tf / FP32_SIMT_TFLOPS, "peak_source": "nominal FP32 SIMT"}
-        l2 = MEASURED_L2_PCT.get((dom, cfg.n, cfg.K, cfg.T, args.precision))
-        if l2 is not None:
-            gbytes = 2 if args.precision == "mixed" else 4
-            roof["l2"] = {"throughput_pct_of_peak": l2[0], "issue_active_pct": l2[1],
-                          "source": "ncu lts__throughput / smsp__issue_active at N=100000 "
-                                    "(profiles/omp_kernel_cfg2.md)",
-                          "support_column_bytes":
-                              float(N) * cfg.K * gbytes * cfg.T * (cfg.T - 1) / 2}
+        gbytes = 2 if args.precision == "mixed" else 4
+        roof["l2"] = {"support_column_bytes": float(N) * cfg.K * gbytes * cfg.T * (cfg.T - 1) / 2}
+        if meas is not None:
+            roof["l2"].update(throughput_pct_of_peak=meas[1], issue_active_pct=meas[2],
+                              source="ncu lts__throughput / smsp__issue_active at N=100000")
     roof["kernel"] = dom
     roof["peak_source"] = pk["src"]
     stage_summary = {k: {"ms_per_launch": round(v[0], 4), "share": round(v[0] * v[1] / sum(

@@ -93,6 +93,7 @@ struct ksvd_handle {
   // host copies of the batched call's tables (kept alive for the asynchronous uploads)
   std::vector<ksvd::GemmDesc> batch_descs;
   std::vector<ksvd::OmpJob> batch_jobs;
+  std::vector<const float*> batch_dicts;   // every job's dictionary (n x K), for the mixed path
 };
 
 namespace {
@@ -237,7 +238,10 @@ ksvd_status store_dict(ksvd_handle* h, const float* Dp, float* D) {
   return KSVD_OK;
 }
 
-int64_t bf16_ld(int n) { return round_up(n, 8); }
+// Row length of the BF16 parts: at least one 64-element TMA box (the columns past n are zero),
+// a multiple of 8 (16-byte rows).  tc_inner(n) is the inner extent the tensor-core GEMM reads.
+int64_t bf16_ld(int n) { return n < 64 ? 64 : round_up(n, 8); }
+int tc_inner(int n) { return n < 64 ? 64 : n; }
 
 bool mixed(const ksvd_handle* h) { return h->p.precision == KSVD_PREC_MIXED; }
 
@@ -282,7 +286,7 @@ ksvd_status gram_padded(ksvd_handle* h, const float* Dp, float* G) {
     int* de = nullptr;
     KSVD_TRY(ensure(h, B_DEVERR, 1, &de));
     KSVD_TRY(split_dict(h, Dp, &d));
-    KSVD_CK(h, launch_gemm_tn_bf16(d, d, G, Kp, Kp, Kp, n, 3, de, h->stream));
+    KSVD_CK(h, launch_gemm_tn_bf16(d, d, G, Kp, Kp, Kp, tc_inner(n), 3, de, h->stream));
     return KSVD_OK;
   }
   KSVD_CK(h, launch_gemm_tn_f32(Dp, n, Dp, n, G, Kp, K, Kp, K, Kp, n, h->stream));
@@ -299,7 +303,7 @@ ksvd_status dtx_padded(ksvd_handle* h, const float* Dp, const float* X, int64_t 
     KSVD_TRY(split_signals(h, X, N, &x));
     StageScope sc(h, KSVD_STAGE_DTX);
     KSVD_TRY(split_dict(h, Dp, &d));
-    KSVD_CK(h, launch_gemm_tn_bf16(d, x, A0, Kp, Kp, N, n, 3, de, h->stream));
+    KSVD_CK(h, launch_gemm_tn_bf16(d, x, A0, Kp, Kp, N, tc_inner(n), 3, de, h->stream));
     return KSVD_OK;
   }
   StageScope sc(h, KSVD_STAGE_DTX);
@@ -327,7 +331,7 @@ ksvd_status dtx_padded_range(ksvd_handle* h, const float* Dp, const float* X, in
     TcOperand d, x;
     KSVD_TRY(split_dict(h, Dp, &d));
     x.hi = hi + s0 * ld; x.lo = lo + s0 * ld; x.ld = ld; x.rows = Nc;
-    KSVD_CK(h, launch_gemm_tn_bf16(d, x, A0 + s0 * Kp, Kp, Kp, Nc, n, 3, de, h->stream));
+    KSVD_CK(h, launch_gemm_tn_bf16(d, x, A0 + s0 * Kp, Kp, Kp, Nc, tc_inner(n), 3, de, h->stream));
     return KSVD_OK;
   }
   StageScope sc(h, KSVD_STAGE_DTX);
@@ -346,11 +350,11 @@ ksvd_status run_omp(ksvd_handle* h, const float* G, const float* A0, int64_t N,
   // dominate the step (measured: slower at T = 8 and 10, faster at T = 16); the autotuner
   // times both.
   uint16_t* gh = nullptr;
-  unsigned* mu = nullptr;
+  float* mu = nullptr;
   const int T = h->p.T;
   if (mixed(h) && T <= 32 && (h->omp_fp16 > 0 || (h->omp_fp16 < 0 && T >= 14))) {
     KSVD_TRY(ensure(h, B_GH, (size_t)h->Kp * h->Kp, &gh));
-    KSVD_TRY(ensure(h, B_MU, 1, &mu));
+    KSVD_TRY(ensure(h, B_MU, (size_t)h->Kp + 1, &mu));
   }
   unsigned long long* q = nullptr;     // grid_mult 0: signals claimed from a work queue
   if (h->omp_grid_mult == 0) KSVD_TRY(ensure(h, B_OMPQ, 1, &q));
@@ -427,6 +431,7 @@ ksvd_status run_error(ksvd_handle* h, const float* Dp, const float* X, int64_t N
   a.bitmap = bm;
   a.rmse_out = rmse_dev_slot;
   a.iter_ctr = iter_ctr;
+  KSVD_TRY(ensure(h, B_DEVERR, 1, &a.dev_err));
   StageScope sc(h, KSVD_STAGE_ERROR);
   KSVD_CK(h, launch_error(a, h->stream));
   h->error_N = N;
@@ -492,8 +497,20 @@ ksvd_status upload_perm(ksvd_handle* h, const int32_t* perms_host, int32_t iters
 
 bool bad_ptr(const void* p) { return p == nullptr; }
 
+// A public call given a null handle records that in the no-handle error slot.
+bool null_handle(const ksvd_handle* h) {
+  if (h) return false;
+  ksvd::set_nohandle_error("a ksvd_* call was given a null handle");
+  return true;
+}
+
 
 }  // namespace
+
+namespace ksvd {
+thread_local std::string g_nohandle_err;
+void set_nohandle_error(const char* msg) { g_nohandle_err = msg ? msg : ""; }
+}  // namespace ksvd
 
 // ============================================================================================
 extern "C" {
@@ -525,10 +542,8 @@ const char* ksvd_status_string(ksvd_status s) {
   return "unknown status";
 }
 
-const char* ksvd_noalloc_last_error();
-
 const char* ksvd_last_error(const ksvd_handle* h) {
-  return h ? h->err.c_str() : ksvd_noalloc_last_error();
+  return h ? h->err.c_str() : ksvd::g_nohandle_err.c_str();
 }
 
 int64_t ksvd_workspace_bytes(const ksvd_handle* h) {
@@ -552,12 +567,21 @@ ksvd_status ksvd_random_permutation(uint64_t seed, int64_t iteration, int32_t K,
 }
 
 ksvd_status ksvd_create(ksvd_handle** out, const ksvd_params* params, void* stream) {
-  if (!out) return KSVD_ERR_INVALID_ARGUMENT;
+  if (!out) {
+    ksvd::set_nohandle_error("ksvd_create: null output pointer");
+    return KSVD_ERR_INVALID_ARGUMENT;
+  }
   *out = nullptr;
   ksvd_status s = check_params(params, nullptr);
-  if (s != KSVD_OK) return s;
+  if (s != KSVD_OK) {
+    ksvd::set_nohandle_error("ksvd_create: invalid or unsupported parameters");
+    return s;
+  }
   ksvd_handle* h = new (std::nothrow) ksvd_handle();
-  if (!h) return KSVD_ERR_OUT_OF_MEMORY;
+  if (!h) {
+    ksvd::set_nohandle_error("ksvd_create: out of host memory");
+    return KSVD_ERR_OUT_OF_MEMORY;
+  }
   h->p = *params;
   h->Kp = omp_padded_k(params->K);
   h->stream = reinterpret_cast<cudaStream_t>(stream);
@@ -566,13 +590,19 @@ ksvd_status ksvd_create(ksvd_handle** out, const ksvd_params* params, void* stre
   if (e != cudaSuccess) {
     delete h;
     cudaGetLastError();
+    ksvd::set_nohandle_error("ksvd_create: no current CUDA device");
     return KSVD_ERR_CUDA;
   }
   int* de = nullptr;
-  if ((s = ensure(h, B_DEVERR, 1, &de)) != KSVD_OK) { delete h; return s; }
+  if ((s = ensure(h, B_DEVERR, 1, &de)) != KSVD_OK) {
+    ksvd::set_nohandle_error(("ksvd_create: " + h->err).c_str());
+    delete h;
+    return s;
+  }
   if (cudaMemsetAsync(de, 0, sizeof(int), h->stream) != cudaSuccess) {
     ksvd_destroy(h);
     cudaGetLastError();
+    ksvd::set_nohandle_error("ksvd_create: cudaMemsetAsync failed");
     return KSVD_ERR_CUDA;
   }
   *out = h;
@@ -614,7 +644,7 @@ void ksvd_destroy(ksvd_handle* h) {
 int64_t ksvd_graph_replays(const ksvd_handle* h) { return h ? h->graph_replays : -1; }
 
 ksvd_status ksvd_read_stage_times(ksvd_handle* h, ksvd_stage_times* out, int32_t reset) {
-  if (!h || !out) return KSVD_ERR_INVALID_ARGUMENT;
+  if (null_handle(h) || !out) return KSVD_ERR_INVALID_ARGUMENT;
   KSVD_CK(h, cudaStreamSynchronize(h->stream));
   collect_stage_times(h);
   for (int i = 0; i < 8; ++i) {
@@ -636,7 +666,7 @@ ksvd_status ksvd_read_stage_times(ksvd_handle* h, ksvd_stage_times* out, int32_t
 }
 
 ksvd_status ksvd_synchronize(ksvd_handle* h) {
-  if (!h) return KSVD_ERR_INVALID_ARGUMENT;
+  if (null_handle(h)) return KSVD_ERR_INVALID_ARGUMENT;
   KSVD_CK(h, cudaStreamSynchronize(h->stream));
   collect_stage_times(h);
   KSVD_CK(h, cudaGetLastError());
@@ -644,13 +674,13 @@ ksvd_status ksvd_synchronize(ksvd_handle* h) {
 }
 
 ksvd_status ksvd_normcols(ksvd_handle* h, float* D) {
-  if (!h || bad_ptr(D)) return KSVD_ERR_INVALID_ARGUMENT;
+  if (null_handle(h) || bad_ptr(D)) return KSVD_ERR_INVALID_ARGUMENT;
   KSVD_CK(h, launch_normcols(D, h->p.n, h->p.K, h->stream));
   return KSVD_OK;
 }
 
 ksvd_status ksvd_remove_row_mean(ksvd_handle* h, float* X, int64_t N, float* mean) {
-  if (!h || bad_ptr(X) || N < 1) return KSVD_ERR_INVALID_ARGUMENT;
+  if (null_handle(h) || bad_ptr(X) || N < 1) return KSVD_ERR_INVALID_ARGUMENT;
   double* part = nullptr;
   float* m = nullptr;
   KSVD_TRY(ensure(h, B_RPART, (size_t)row_mean_blocks(N) * h->p.n, &part));
@@ -665,13 +695,13 @@ ksvd_status ksvd_remove_row_mean(ksvd_handle* h, float* X, int64_t N, float* mea
 int64_t ksvd_perm_draws(const ksvd_handle* h) { return h ? h->perm_draws : -1; }
 
 ksvd_status ksvd_set_perm_draws(ksvd_handle* h, int64_t draws) {
-  if (!h || draws < 0) return KSVD_ERR_INVALID_ARGUMENT;
+  if (null_handle(h) || draws < 0) return KSVD_ERR_INVALID_ARGUMENT;
   h->perm_draws = draws;
   return KSVD_OK;
 }
 
 ksvd_status ksvd_gram(ksvd_handle* h, const float* D, float* G) {
-  if (!h || bad_ptr(D) || bad_ptr(G)) return KSVD_ERR_INVALID_ARGUMENT;
+  if (null_handle(h) || bad_ptr(D) || bad_ptr(G)) return KSVD_ERR_INVALID_ARGUMENT;
   const int n = h->p.n, K = h->p.K;
   if (mixed(h)) {
     float *Dp = nullptr;
@@ -680,7 +710,7 @@ ksvd_status ksvd_gram(ksvd_handle* h, const float* D, float* G) {
     KSVD_TRY(ensure(h, B_DEVERR, 1, &de));
     KSVD_TRY(load_dict(h, D, &Dp));
     KSVD_TRY(split_dict(h, Dp, &d));
-    KSVD_CK(h, launch_gemm_tn_bf16(d, d, G, K, K, K, n, 3, de, h->stream));
+    KSVD_CK(h, launch_gemm_tn_bf16(d, d, G, K, K, K, tc_inner(n), 3, de, h->stream));
     return KSVD_OK;
   }
   KSVD_CK(h, launch_gemm_tn_f32(D, n, D, n, G, K, K, K, K, K, n, h->stream));
@@ -688,7 +718,7 @@ ksvd_status ksvd_gram(ksvd_handle* h, const float* D, float* G) {
 }
 
 ksvd_status ksvd_dtx(ksvd_handle* h, const float* D, const float* X, int64_t N, float* A0) {
-  if (!h || bad_ptr(D) || bad_ptr(X) || bad_ptr(A0) || N < 0) return KSVD_ERR_INVALID_ARGUMENT;
+  if (null_handle(h) || bad_ptr(D) || bad_ptr(X) || bad_ptr(A0) || N < 0) return KSVD_ERR_INVALID_ARGUMENT;
   const int n = h->p.n, K = h->p.K;
   if (mixed(h)) {
     float* Dp = nullptr;
@@ -699,7 +729,7 @@ ksvd_status ksvd_dtx(ksvd_handle* h, const float* D, const float* X, int64_t N, 
     KSVD_TRY(split_dict(h, Dp, &d));
     KSVD_TRY(split_signals(h, X, N, &x));
     drop_xsplit(h);
-    KSVD_CK(h, launch_gemm_tn_bf16(d, x, A0, K, K, N, n, 3, de, h->stream));
+    KSVD_CK(h, launch_gemm_tn_bf16(d, x, A0, K, K, N, tc_inner(n), 3, de, h->stream));
     return KSVD_OK;
   }
   KSVD_CK(h, launch_gemm_tn_f32(D, n, X, n, A0, K, K, K, N, N, n, h->stream));
@@ -709,7 +739,7 @@ ksvd_status ksvd_dtx(ksvd_handle* h, const float* D, const float* X, int64_t N, 
 ksvd_status ksvd_omp_gram(ksvd_handle* h, const float* G, const float* A0, int64_t N,
                           const float* xnorm2, const float* eps2, int32_t* idx, float* coef,
                           int32_t* nnz) {
-  if (!h || bad_ptr(G) || bad_ptr(A0) || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || N < 0)
+  if (null_handle(h) || bad_ptr(G) || bad_ptr(A0) || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || N < 0)
     return KSVD_ERR_INVALID_ARGUMENT;
   if (eps2 && !xnorm2) return fail(h, KSVD_ERR_INVALID_ARGUMENT, "eps2 needs xnorm2%s");
   if (N == 0) return KSVD_OK;
@@ -726,7 +756,7 @@ ksvd_status ksvd_omp_gram(ksvd_handle* h, const float* G, const float* A0, int64
 
 ksvd_status ksvd_omp(ksvd_handle* h, const float* D, const float* X, int64_t N, const float* eps2,
                      int32_t* idx, float* coef, int32_t* nnz) {
-  if (!h || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || N < 0)
+  if (null_handle(h) || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || N < 0)
     return KSVD_ERR_INVALID_ARGUMENT;
   if (N == 0) return KSVD_OK;
   drop_xsplit(h);
@@ -805,6 +835,7 @@ ksvd_status batched_omp_plan(ksvd_handle* h, const ksvd_problem* probs, int32_t 
   auto& jobs = h->batch_jobs;
   descs.assign(2 * (size_t)nprob, GemmDesc{});
   jobs.assign((size_t)nprob, OmpJob{});
+  h->batch_dicts.assign((size_t)nprob, nullptr);
   int64_t tiles = 0, chunks = 0;
   int nd = 0, nj = 0;
   const int chunk = h->batch_chunk > 0 ? h->batch_chunk : omp_batch_chunk();
@@ -816,6 +847,7 @@ ksvd_status batched_omp_plan(ksvd_handle* h, const ksvd_problem* probs, int32_t 
     float* A0 = Aall + aoff[i];
     tiles = gemm_desc_fill(descs[nd++], q.D, q.n, q.D, q.n, G, kp, q.K, kp, q.K, kp, q.n, tiles);
     tiles = gemm_desc_fill(descs[nd++], q.D, q.n, q.X, q.n, A0, kp, q.K, kp, q.N, q.N, q.n, tiles);
+    h->batch_dicts[nj] = q.D;
     OmpJob& j = jobs[nj++];
     j.G = G; j.ldg = kp; j.A0 = A0; j.lda = kp; j.X = q.X; j.ldx = q.n; j.eps2 = q.eps2;
     j.idx = q.idx; j.coef = q.coef; j.nnz = q.nnz; j.N = q.N; j.chunk_begin = chunks;
@@ -832,12 +864,46 @@ ksvd_status batched_omp_plan(ksvd_handle* h, const ksvd_problem* probs, int32_t 
   return KSVD_OK;
 }
 
-// The grouped GEMM and the persistent Batch-OMP launch of an uploaded plan.
+// Mixed precision: every problem's G = D'D and alpha0 = D'X on the tensor cores (BF16 hi/lo
+// parts, three passes, FP32 accumulation, as the single-problem mixed path), one problem after
+// another on the handle's stream; the split buffers are shared by the problems in turn.
+ksvd_status batched_gemms_tc(ksvd_handle* h, const BatchPlan& pl) {
+  int64_t dmax = 0, xmax = 0;
+  for (int j = 0; j < pl.nj; ++j) {
+    const OmpJob& jb = h->batch_jobs[j];
+    const int64_t ld = bf16_ld(jb.n);
+    dmax = std::max<int64_t>(dmax, (int64_t)jb.ldg * ld);
+    xmax = std::max<int64_t>(xmax, jb.N * ld);
+  }
+  uint16_t *dhi = nullptr, *dlo = nullptr, *xhi = nullptr, *xlo = nullptr;
+  KSVD_TRY(ensure(h, B_DHI, (size_t)dmax, &dhi));
+  KSVD_TRY(ensure(h, B_DLO, (size_t)dmax, &dlo));
+  KSVD_TRY(ensure(h, B_XHI, (size_t)xmax, &xhi));
+  KSVD_TRY(ensure(h, B_XLO, (size_t)xmax, &xlo));
+  drop_xsplit(h);                       // the X split buffers now hold other signals
+  for (int j = 0; j < pl.nj; ++j) {
+    const OmpJob& jb = h->batch_jobs[j];
+    const int kp = (int)jb.ldg, n = jb.n;
+    const int64_t ld = bf16_ld(n);
+    KSVD_CK(h, launch_split_bf16(h->batch_dicts[j], n, jb.K, n, dhi, dlo, ld, kp, h->stream));
+    KSVD_CK(h, launch_split_bf16(jb.X, jb.ldx, jb.N, n, xhi, xlo, ld, jb.N, h->stream));
+    const TcOperand d{dhi, dlo, ld, kp}, x{xhi, xlo, ld, jb.N};
+    KSVD_CK(h, launch_gemm_tn_bf16(d, d, const_cast<float*>(jb.G), kp, kp, kp, tc_inner(n), 3,
+                                   pl.de, h->stream));
+    KSVD_CK(h, launch_gemm_tn_bf16(d, x, const_cast<float*>(jb.A0), kp, kp, jb.N, tc_inner(n), 3,
+                                   pl.de, h->stream));
+  }
+  return KSVD_OK;
+}
+
+// The GEMMs (grouped FP32 launch, or per-problem tensor-core products for the mixed path) and
+// the persistent Batch-OMP launch of an uploaded plan.
 ksvd_status batched_omp_launch(ksvd_handle* h, const BatchPlan& pl) {
   if (pl.nj == 0) return KSVD_OK;
   {
     StageScope sc(h, KSVD_STAGE_DTX);
-    KSVD_CK(h, launch_gemm_tn_f32_grouped(pl.ddev, pl.nd, pl.tiles, h->stream));
+    if (mixed(h)) KSVD_TRY(batched_gemms_tc(h, pl));
+    else KSVD_CK(h, launch_gemm_tn_f32_grouped(pl.ddev, pl.nd, pl.tiles, h->stream));
   }
   StageScope sc(h, KSVD_STAGE_OMP);
   KSVD_CK(h, launch_omp_batched(pl.jdev, pl.nj, pl.chunks, pl.tmax, pl.chunk, pl.queue, pl.de,
@@ -848,7 +914,7 @@ ksvd_status batched_omp_launch(ksvd_handle* h, const BatchPlan& pl) {
 }  // namespace
 
 ksvd_status ksvd_batched_omp(ksvd_handle* h, const ksvd_problem* probs, int32_t nprob) {
-  if (!h || nprob < 0 || (nprob > 0 && !probs)) return KSVD_ERR_INVALID_ARGUMENT;
+  if (null_handle(h) || nprob < 0 || (nprob > 0 && !probs)) return KSVD_ERR_INVALID_ARGUMENT;
   if (nprob == 0) return KSVD_OK;
   BatchPlan pl;
   KSVD_TRY(batched_omp_plan(h, probs, nprob, &pl));
@@ -963,7 +1029,7 @@ extern "C" {
 // the handle's atom-order stream and stage state are restored.
 ksvd_status ksvd_autotune(ksvd_handle* h, const float* D, const float* X, int64_t N,
                           ksvd_tuning* out) {
-  if (!h || bad_ptr(D) || bad_ptr(X) || N < 1) return KSVD_ERR_INVALID_ARGUMENT;
+  if (null_handle(h) || bad_ptr(D) || bad_ptr(X) || N < 1) return KSVD_ERR_INVALID_ARGUMENT;
   if ((int64_t)N * h->p.T > 0x7fffffffLL)
     return fail(h, KSVD_ERR_UNSUPPORTED, "N*T must stay below 2^31%s");
   const int n = h->p.n, Kp = h->Kp, T = h->p.T;
@@ -1041,7 +1107,7 @@ ksvd_status ksvd_autotune(ksvd_handle* h, const float* D, const float* X, int64_
 // timed on the given problems.
 ksvd_status ksvd_autotune_batched(ksvd_handle* h, const ksvd_problem* probs, int32_t nprob,
                                   ksvd_tuning* out) {
-  if (!h || nprob < 1 || !probs) return KSVD_ERR_INVALID_ARGUMENT;
+  if (null_handle(h) || nprob < 1 || !probs) return KSVD_ERR_INVALID_ARGUMENT;
   const bool prof = h->profiling();
   h->p.flags &= ~KSVD_FLAG_PROFILE;
   ksvd_status st = KSVD_OK;
@@ -1105,13 +1171,13 @@ ksvd_status ksvd_autotune_batched(ksvd_handle* h, const ksvd_problem* probs, int
 }
 
 ksvd_status ksvd_get_tuning(const ksvd_handle* h, ksvd_tuning* out) {
-  if (!h || !out) return KSVD_ERR_INVALID_ARGUMENT;
+  if (null_handle(h) || !out) return KSVD_ERR_INVALID_ARGUMENT;
   fill_tuning(h, out);
   return KSVD_OK;
 }
 
 ksvd_status ksvd_set_tuning(ksvd_handle* h, const ksvd_tuning* t) {
-  if (!h || !t || t->omp_grid_mult < 0 || t->omp_grid_mult > 64 || t->sweep_ctas < 0 ||
+  if (null_handle(h) || !t || t->omp_grid_mult < 0 || t->omp_grid_mult > 64 || t->sweep_ctas < 0 ||
       t->batch_chunk < 0 || t->batch_chunk > 4096 || t->omp_fp16 < -1 || t->omp_fp16 > 1)
     return KSVD_ERR_INVALID_ARGUMENT;
   h->omp_fp16 = t->omp_fp16;
@@ -1126,7 +1192,7 @@ ksvd_status ksvd_set_tuning(ksvd_handle* h, const ksvd_tuning* t) {
 ksvd_status ksvd_update_dictionary(ksvd_handle* h, float* D, const float* X, int64_t N,
                                    const int32_t* idx, float* coef, const int32_t* nnz,
                                    const int32_t* perm) {
-  if (!h || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || N < 1)
+  if (null_handle(h) || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || N < 1)
     return KSVD_ERR_INVALID_ARGUMENT;
   if ((int64_t)N * h->p.T > 0x7fffffffLL)
     return fail(h, KSVD_ERR_UNSUPPORTED, "N*T must stay below 2^31%s");
@@ -1146,7 +1212,7 @@ ksvd_status ksvd_update_dictionary(ksvd_handle* h, float* D, const float* X, int
 ksvd_status ksvd_error(ksvd_handle* h, const float* D, const float* X, int64_t N,
                        const int32_t* idx, const float* coef, const int32_t* nnz, float* err,
                        double* rmse) {
-  if (!h || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || N < 1)
+  if (null_handle(h) || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || N < 1)
     return KSVD_ERR_INVALID_ARGUMENT;
   float* Dp = nullptr;
   double* rd = nullptr;
@@ -1169,7 +1235,7 @@ ksvd_status ksvd_error(ksvd_handle* h, const float* D, const float* X, int64_t N
 ksvd_status ksvd_clear_dict(ksvd_handle* h, float* D, const float* X, int64_t N,
                             const int32_t* idx, const float* coef, const int32_t* nnz,
                             int32_t* cleared) {
-  if (!h || bad_ptr(D) || bad_ptr(X) || N < 1) return KSVD_ERR_INVALID_ARGUMENT;
+  if (null_handle(h) || bad_ptr(D) || bad_ptr(X) || N < 1) return KSVD_ERR_INVALID_ARGUMENT;
   (void)idx; (void)coef; (void)nnz;
   if (h->update_N != N || h->error_N != N)
     return fail(h, KSVD_ERR_STATE,
@@ -1346,7 +1412,7 @@ struct EpsScope {
 ksvd_status iterate_impl(ksvd_handle* h, float* D, const float* X, int64_t N, int32_t iters,
                          const int32_t* perms, const float* eps2, int32_t* idx, float* coef,
                          int32_t* nnz, double* rmse) {
-  if (!h || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || N < 1 ||
+  if (null_handle(h) || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || N < 1 ||
       iters < 0)
     return KSVD_ERR_INVALID_ARGUMENT;
   EpsScope eps_scope{h};
@@ -1424,7 +1490,7 @@ ksvd_status iterate_impl(ksvd_handle* h, float* D, const float* X, int64_t N, in
 // the second and later iterations replay one captured graph of the whole batched iteration.
 ksvd_status ksvd_batched_iterate(ksvd_handle* h, ksvd_problem* probs, int32_t nprob,
                                  int32_t iters, double* rmse) {
-  if (!h || nprob < 0 || (nprob > 0 && !probs) || iters < 0) return KSVD_ERR_INVALID_ARGUMENT;
+  if (null_handle(h) || nprob < 0 || (nprob > 0 && !probs) || iters < 0) return KSVD_ERR_INVALID_ARGUMENT;
   if (nprob == 0 || iters == 0) return KSVD_OK;
   if (iters > 1024) return fail(h, KSVD_ERR_UNSUPPORTED, "at most 1024 iterations per call%s");
   for (int32_t i = 0; i < nprob; ++i)
@@ -1527,11 +1593,11 @@ ksvd_status ksvd_batched_iterate(ksvd_handle* h, ksvd_problem* probs, int32_t np
   return check_dev_err(h);
 }
 
-ksvd_status ksvd_iterate_host(ksvd_handle* h, float* D, const float* X, int64_t N, int32_t iters,
-                              const int32_t* perms, int32_t* idx, float* coef, int32_t* nnz,
-                              double* rmse) {
-  if (!h || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || N < 1)
-    return KSVD_ERR_INVALID_ARGUMENT;
+// Body of ksvd_iterate_host; a return before its final synchronisation may leave copies that
+// read X or write idx/coef/nnz queued on the handle's stream or the copy stream.
+static ksvd_status iterate_host_body(ksvd_handle* h, float* D, const float* X, int64_t N,
+                                     int32_t iters, const int32_t* perms, int32_t* idx,
+                                     float* coef, int32_t* nnz, double* rmse) {
   const int n = h->p.n, K = h->p.K, T = h->p.T;
   float *dX = nullptr, *dD = nullptr, *dC = nullptr;
   int32_t *dI = nullptr, *dN = nullptr;
@@ -1597,9 +1663,27 @@ ksvd_status ksvd_iterate_host(ksvd_handle* h, float* D, const float* X, int64_t 
   return KSVD_OK;
 }
 
+ksvd_status ksvd_iterate_host(ksvd_handle* h, float* D, const float* X, int64_t N, int32_t iters,
+                              const int32_t* perms, int32_t* idx, float* coef, int32_t* nnz,
+                              double* rmse) {
+  if (null_handle(h) || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || N < 1)
+    return KSVD_ERR_INVALID_ARGUMENT;
+  const ksvd_status st = iterate_host_body(h, D, X, N, iters, perms, idx, coef, nnz, rmse);
+  if (st != KSVD_OK) {
+    // no copy may touch the caller's host buffers after the call returns: drain both streams
+    // (their own errors are already reported by st)
+    cudaStreamSynchronize(h->stream);
+    if (h->inflow.cstream) cudaStreamSynchronize(h->inflow.cstream);
+    cudaGetLastError();
+    h->inflow.active = false;
+    h->inflow.drain = false;
+  }
+  return st;
+}
+
 ksvd_status ksvd_code_fixed(ksvd_handle* h, const float* D, const float* X, int64_t N,
                             const int32_t* idx, const int32_t* nnz, float* coef, float* chol) {
-  if (!h || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(nnz) || bad_ptr(coef) || N < 0)
+  if (null_handle(h) || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(nnz) || bad_ptr(coef) || N < 0)
     return KSVD_ERR_INVALID_ARGUMENT;
   if (N == 0) return KSVD_OK;
   float *Dp = nullptr, *G = nullptr;
@@ -1615,7 +1699,7 @@ ksvd_status ksvd_code_fixed(ksvd_handle* h, const float* D, const float* X, int6
 
 ksvd_status ksvd_refine_coefs(ksvd_handle* h, const float* D, const float* X, int64_t N,
                               const int32_t* idx, const int32_t* nnz, float* coef, double* coef64) {
-  if (!h || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(nnz) || bad_ptr(coef) || N < 0)
+  if (null_handle(h) || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(nnz) || bad_ptr(coef) || N < 0)
     return KSVD_ERR_INVALID_ARGUMENT;
   if (N == 0) return KSVD_OK;
   float *Dp = nullptr, *G = nullptr;
@@ -1632,7 +1716,7 @@ ksvd_status ksvd_refine_coefs(ksvd_handle* h, const float* D, const float* X, in
 ksvd_status ksvd_code_backward(ksvd_handle* h, const float* D, const float* X, int64_t N,
                                const int32_t* idx, const int32_t* nnz, const float* coef,
                                const float* chol, const float* dcoef, float* dD, float* dX) {
-  if (!h || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(nnz) || bad_ptr(coef) ||
+  if (null_handle(h) || bad_ptr(D) || bad_ptr(X) || bad_ptr(idx) || bad_ptr(nnz) || bad_ptr(coef) ||
       bad_ptr(chol) || bad_ptr(dcoef) || N < 0)
     return KSVD_ERR_INVALID_ARGUMENT;
   if (N == 0) return KSVD_OK;
@@ -1643,7 +1727,7 @@ ksvd_status ksvd_code_backward(ksvd_handle* h, const float* D, const float* X, i
 
 ksvd_status ksvd_dense_gamma(ksvd_handle* h, int64_t N, const int32_t* idx, const float* coef,
                              const int32_t* nnz, float* gamma) {
-  if (!h || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || bad_ptr(gamma) || N < 0)
+  if (null_handle(h) || bad_ptr(idx) || bad_ptr(coef) || bad_ptr(nnz) || bad_ptr(gamma) || N < 0)
     return KSVD_ERR_INVALID_ARGUMENT;
   KSVD_CK(h, launch_dense_gamma(idx, coef, nnz, N, h->p.T, h->p.K, gamma, h->stream));
   return KSVD_OK;

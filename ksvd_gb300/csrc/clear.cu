@@ -33,6 +33,7 @@ error_kernel(ErrorArgs A) {
   double sum = 0.0;
   float bv = -1.f;
   int64_t bi = INT64_MAX;
+  bool bad = false;
   for (int64_t s = s0 + w; s < s1; s += kErrWarps) {
     float acc[NPL];
     const float* x = A.X + s * n;
@@ -51,6 +52,7 @@ error_kernel(ErrorArgs A) {
       const int t = lane + 32 * u;
       const int k = t < nz ? A.idx[s * T + t] : -1;
       const bool ok = k >= 0 && k < A.K;
+      bad |= t < nz && !ok;
       kk[u] = ok ? k : -1;
       gg[u] = ok ? A.coef[s * T + t] : 0.f;
     }
@@ -75,6 +77,7 @@ error_kernel(ErrorArgs A) {
     if (lane == 0) A.err[s] = em;
     if (em > bv) { bv = em; bi = s; }       // s ascends within the warp: first maximum kept
   }
+  if (__any_sync(KSVD_FULL_MASK, bad) && lane == 0 && A.dev_err) atomicOr(A.dev_err, kDevErrBounds);
   if (lane == 0) { wsum[w] = sum; wval[w] = bv; widx[w] = bi; }
   __syncthreads();
   if (threadIdx.x == 0) {

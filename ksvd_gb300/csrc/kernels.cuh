@@ -41,15 +41,17 @@ int omp_padded_k(int K);
 // grid_mult: resident CTAs per SM x grid_mult blocks at most, signals assigned grid-stride; 0 with
 // a queue (one zeroed counter): one resident grid whose warps claim signals from the queue (0
 // without a queue: 8; the autotuner's knob)
-// Gh/mu (mixed path, T <= 32): FP16 copy of G and its coherence from launch_gram_half; the alpha
-// update then reads Gh and resolves near ties in FP32 (the selection is the FP32 Batch-OMP's).
+// Gh/mu (mixed path, T <= 32): FP16 copy of G and its per-column coherence from
+// launch_gram_half; the alpha update then reads Gh and resolves near ties in FP32 (the selection
+// is the FP32 Batch-OMP's).
 cudaError_t launch_omp(const float* G, int64_t ldg, const float* A0, int64_t lda, int K,
                        int64_t N, int T, const float* xnorm2, const float* eps2, int32_t* idx,
                        float* coef, int32_t* nnz, int* dev_err, cudaStream_t st,
                        int grid_mult = 0, const uint16_t* Gh = nullptr,
-                       const unsigned* mu = nullptr, unsigned long long* queue = nullptr);
-// Gh = FP16(G) (Kp x Kp, same ldg) and mu = max off-diagonal |G(i, j)|, i, j < K.
-cudaError_t launch_gram_half(const float* G, int64_t ldg, int K, uint16_t* Gh, unsigned* mu,
+                       const float* mu = nullptr, unsigned long long* queue = nullptr);
+// Gh = FP16(G) (Kp x Kp, same ldg), mu_col[c] = max_{k != c, k < K} |G(k, c)| (zero past K) and
+// mu_col[Kp] = max_k |G(k, k) - 1| (Kp + 1 floats): what the FP16 update's error bound uses.
+cudaError_t launch_gram_half(const float* G, int64_t ldg, int K, uint16_t* Gh, float* mu_col,
                              cudaStream_t st);
 
 // ---- misc (misc.cu) ---------------------------------------------------------------------------
@@ -117,6 +119,7 @@ struct ErrorArgs {
   int64_t* bucket_idx;   // per error block: its signal (lowest on ties)
   double* rmse_out;      // device scalar (rmse_out[*iter_ctr] when iter_ctr is set)
   const int* iter_ctr;   // nullable
+  int* dev_err;          // nullable: kDevErrBounds when a used slot holds an index outside [0, K)
 };
 int64_t error_block_count(int64_t N);
 cudaError_t launch_error(const ErrorArgs& a, cudaStream_t st);
@@ -199,5 +202,9 @@ cudaError_t launch_code_backward(const float* D, int n, int K, const float* X, i
                                  const int32_t* idx, const int32_t* nnz, const float* coef,
                                  const float* chol, const float* dcoef, float* dD, float* dX,
                                  cudaStream_t st);
+
+// The last failure of a call that had no handle to record it in (a null handle, a failed
+// ksvd_create, ksvd_rmse_noalloc), per host thread; ksvd_last_error(NULL) returns it.
+void set_nohandle_error(const char* msg);
 
 }  // namespace ksvd

@@ -7,26 +7,32 @@
 // implicit device synchronisation of cudaMalloc/cudaFree is not acceptable.  ksvd_error needs a
 // handle, and a handle holds device workspace; this entry point needs neither.  The caller passes
 // the inputs (D, X, the sparse code) and receives the RMSE on the host; the only scratch -- one
-// FP64 partial sum per 256-signal block plus the result -- lives in the file-scope array below,
-// which every GPU that loads this library holds until the process exits.
+// FP64 partial sum per 256-signal block plus the result and a bad-index flag -- lives in the
+// file-scope array below, which every GPU that loads this library holds until the process exits.
 //
-// Set-up: the first call on a device resolves the array's device address with
-// cudaGetSymbolAddress while that device is current (host code may not use the array's name as
-// a device address); later calls on that device reuse it.  That first call should therefore come
-// before any stream capture.  Calls share the array: two calls whose kernels overlap on the same
-// GPU (different streams or threads) race on it.  Every partial sum is written before it is read,
-// so nothing has to be cleared between calls.
+// Set-up: host code may not use the array's name as a device address, so every call that is not
+// made under stream capture looks the address up with cudaGetSymbolAddress while the call's
+// device is current (after a cudaDeviceReset the library's device code is loaded again and the
+// array may move); a call under capture reuses the last address looked up on that device.  The
+// first call on a device also makes the CUDA driver load this library's device code if nothing
+// has yet, which makes the array resident; that first call should therefore come before any
+// stream capture.  Calls share the array: two calls whose kernels overlap on the same GPU
+// (different streams or threads) race on it.  Every slot a call reads is written earlier in the
+// same call, so nothing has to be cleared between calls.
 #include <mutex>
 #include <string>
 
 #include "../../include/ksvd_gb300.h"
 #include "common.cuh"
+#include "kernels.cuh"
 
 namespace {
 
 constexpr int kNoallocBlock = 256;       // signals per block (8 warps, one signal per warp)
 constexpr int kNoallocBlocks = 65536;    // -> N <= 16,777,216
 
+// [0, kNoallocBlocks): per-block partial sums (negative: the block met an atom index outside
+// [0, K) in a used slot); [kNoallocBlocks]: the RMSE; [kNoallocBlocks + 1]: 1 if any block did
 __device__ __align__(256) double g_rmse_scratch[kNoallocBlocks + 2];
 
 // The RMSE half of the error kernel (clear.cu) with its per-block sums written to `part`:
@@ -38,10 +44,12 @@ rmse_noalloc_partial_kernel(const float* __restrict__ X, const float* __restrict
                             const float* __restrict__ coef, const int32_t* __restrict__ nnz,
                             double* __restrict__ part) {
   __shared__ double wsum[8];
+  __shared__ int wbad[8];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t b = blockIdx.x;
   const int64_t s0 = b * kNoallocBlock, s1 = min(N, s0 + kNoallocBlock);
   double sum = 0.0;
+  bool bad = false;
   for (int64_t s = s0 + w; s < s1; s += 8) {
     float acc[NPL];
     const float* x = X + s * n;
@@ -53,7 +61,7 @@ rmse_noalloc_partial_kernel(const float* __restrict__ X, const float* __restrict
     const int nz = min(nnz[s], T);
     for (int t = 0; t < nz; ++t) {
       const int k = idx[s * T + t];
-      if (k < 0 || k >= K) continue;
+      if (k < 0 || k >= K) { bad = true; continue; }
       const float g = coef[s * T + t];
       const float* d = D + (int64_t)k * n;
 #pragma unroll
@@ -67,12 +75,14 @@ rmse_noalloc_partial_kernel(const float* __restrict__ X, const float* __restrict
     for (int i = 0; i < NPL; ++i) e = fmaf(acc[i], acc[i], e);
     sum += (double)ksvd::warp_sum(e);
   }
-  if (lane == 0) wsum[w] = sum;
+  const bool wb = __any_sync(KSVD_FULL_MASK, bad);
+  if (lane == 0) { wsum[w] = sum; wbad[w] = wb; }
   __syncthreads();
   if (threadIdx.x == 0) {
     double t = 0.0;
-    for (int ww = 0; ww < 8; ++ww) t += wsum[ww];
-    part[b] = t;
+    int nb = 0;
+    for (int ww = 0; ww < 8; ++ww) { t += wsum[ww]; nb |= wbad[ww]; }
+    part[b] = nb ? -1.0 : t;
   }
 }
 
@@ -80,7 +90,13 @@ __global__ void rmse_noalloc_final_kernel(const double* __restrict__ part, int64
                                           double denom, double* __restrict__ out) {
   __shared__ double red[32];
   double t = 0.0;
-  for (int64_t i = threadIdx.x; i < nb; i += blockDim.x) t += part[i];
+  bool bad = false;
+  for (int64_t i = threadIdx.x; i < nb; i += blockDim.x) {
+    const double v = part[i];
+    bad |= v < 0.0;
+    t += v;
+  }
+  bad = __syncthreads_or(bad);
   t = ksvd::warp_sum_d(t);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (lane == 0) red[w] = t;
@@ -88,7 +104,10 @@ __global__ void rmse_noalloc_final_kernel(const double* __restrict__ part, int64
   if (w == 0) {
     t = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
     t = ksvd::warp_sum_d(t);
-    if (lane == 0) *out = sqrt(t / denom);
+    if (lane == 0) {
+      out[0] = bad ? 0.0 : sqrt(t / denom);
+      out[1] = bad ? 1.0 : 0.0;
+    }
   }
 }
 
@@ -111,16 +130,12 @@ cudaError_t launch_rmse_noalloc(const float* X, const float* D, int n, int K, in
 std::mutex g_mu;
 double* g_scratch_ptr[128] = {nullptr};
 
-thread_local std::string g_noalloc_err;
-
 ksvd_status fail(ksvd_status s, const char* msg) {
-  g_noalloc_err = msg;
+  ksvd::set_nohandle_error(msg);
   return s;
 }
 
 }  // namespace
-
-extern "C" const char* ksvd_noalloc_last_error() { return g_noalloc_err.c_str(); }
 
 extern "C" ksvd_status ksvd_rmse_noalloc(int32_t n, int32_t K, int32_t T, const float* D,
                                          const float* X, int64_t N, const int32_t* idx,
@@ -143,10 +158,18 @@ extern "C" ksvd_status ksvd_rmse_noalloc(int32_t n, int32_t K, int32_t T, const 
     cudaGetLastError();
     return fail(KSVD_ERR_CUDA, "ksvd_rmse_noalloc: no current CUDA device");
   }
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  // look the address up again unless the stream is being captured (a reset device reloads the
+  // library's device code); under capture the last address looked up on this device is used
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) {
+    cudaGetLastError();
+    cap = cudaStreamCaptureStatusActive;
+  }
   double* scratch = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_ptr[dev]) {
+    if (cap == cudaStreamCaptureStatusNone || !g_scratch_ptr[dev]) {
       void* p = nullptr;
       e = cudaGetSymbolAddress(&p, g_rmse_scratch);
       if (e != cudaSuccess || !p) {
@@ -157,17 +180,22 @@ extern "C" ksvd_status ksvd_rmse_noalloc(int32_t n, int32_t K, int32_t T, const 
     }
     scratch = g_scratch_ptr[dev];
   }
-  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  double res[2] = {0.0, 0.0};
   e = launch_rmse_noalloc(X, D, n, K, T, N, idx, coef, nnz, scratch, nb,
                           scratch + kNoallocBlocks, st);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(rmse, scratch + kNoallocBlocks, sizeof(double), cudaMemcpyDeviceToHost, st);
+    e = cudaMemcpyAsync(res, scratch + kNoallocBlocks, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                        st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
-    g_noalloc_err = std::string("ksvd_rmse_noalloc: ") + cudaGetErrorString(e);
+    const std::string msg = std::string("ksvd_rmse_noalloc: ") + cudaGetErrorString(e);
     cudaGetLastError();
-    return KSVD_ERR_CUDA;
+    return fail(KSVD_ERR_CUDA, msg.c_str());
   }
-  g_noalloc_err.clear();
+  if (res[1] != 0.0)
+    return fail(KSVD_ERR_INVALID_ARGUMENT,
+                "ksvd_rmse_noalloc: sparse code holds an atom index outside [0, K)");
+  *rmse = res[0];
+  ksvd::set_nohandle_error("");
   return KSVD_OK;
 }

@@ -102,6 +102,25 @@ __device__ __forceinline__ void fma2_f16_f32(uint32_t g, unsigned short c, float
 // per step; more candidates (or a maximum too small to trust) recompute the whole alpha in FP32.
 constexpr int kMaxCand = 8;
 
+// Rigorous bound on |alpha~_k - alpha_k| for an atom k outside the support of i atoms, where
+// alpha~_k = fl(alpha0_k - S acc_k), acc_k the FP32-accumulated sum of fp16(G(k, I_r)) c~_r with
+// c~_r = fp16(c_r / S) (S = 2^ex > ||c||_1), and alpha_k = fl(alpha0_k - s_k) with s_k the FP32
+// kernel's FMA chain over the same terms.  With |G(k, I_r)| <= mu_r (the coherence of support
+// column I_r), w1 = sum_r mu_r |c_r| and cl1 = ||c||_1:
+//   FP16 rounding: |fp16(g) - g| <= 2^-11 |g| + 2^-25, |c~ S - c| <= 2^-11 |c| + 2^-25 S, so
+//   the products differ by <= 2^-10 |g c| + 2^-25 |c| (1 + 2^-11) + 2^-25 S |g| (1 + 2^-11),
+//   and sum_r S mu_r <= 2 i cl1;
+//   the two FMA chains of i terms add <= 2 i 2^-24 (1 + 2^-9) w1 (products exact in FP32);
+//   the final subtractions add <= 2^-24 (|alpha~_k| + |alpha_k|) <= 2^-23 a (1 + 2^-9),
+//   a = the largest |alpha~| over the atoms.
+// Generous constants: eb = w1 (2^-10 + (i + 2) 2^-22) + cl1 (2^-24 + (i + 1) 2^-23) + a 2^-22.
+// For a support atom k = I_q the column's own term has |G(k, k)| <= 1 + d_q (d_q = |G(k, k) - 1|)
+// instead of mu_q: its bound is eb + 2^-9 (1 + d_q) |c_q|.
+__device__ __forceinline__ float alpha_bound(float w1, float cl1, int i, float a) {
+  return w1 * (ldexpf(1.f, -10) + (float)(i + 2) * ldexpf(1.f, -22)) +
+         cl1 * (ldexpf(1.f, -24) + (float)(i + 1) * ldexpf(1.f, -23)) + a * ldexpf(1.f, -22);
+}
+
 // Batch-OMP of one signal by one warp.  a0col: the signal's alpha0 column (Kp = 32*KPL rows,
 // rows >= K zero); L: the Cholesky factor (first T rows of the TMAX layout), a0s: 32*KPL floats
 // and cand: kMaxCand ints of this warp's shared memory.  emode: stop once ||x||^2 - ||y||^2 <= e2
@@ -109,16 +128,22 @@ constexpr int kMaxCand = 8;
 //
 // H16 (mixed path): alpha = alpha0 - G(:, I) c is formed from an FP16 copy Gh of G (half the L2
 // bytes of the re-read support columns; c scaled by a power of two into FP16 range, products
-// accumulated in FP32).  Its error per atom is below 2^-10 sum_r |G(k, I_r) c_r|; the allowance
-// errb = tol * ||c||_1 (tol = 2^-12 mu + 2^-18, mu the dictionary's coherence) is a quarter of
-// that worst case and ~10x the rounding error's spread; the 2^-18 floor covers FP16 subnormals
-// and the FP32 summation order.  Every atom whose approximate |alpha| lies within 2 errb of the
-// maximum is re-evaluated in FP32 with exactly the FP32 path's operations, so the selection, the
-// stop tests and the coefficients are those of the FP32 Batch-OMP; with more than kMaxCand
-// candidates, or a maximum below 4 errb, the step's alpha is recomputed in FP32.
+// accumulated in FP32), with the rigorous per-atom error bound eb of alpha_bound() (mu_col: the
+// per-column coherence).  The FP32 kernel's choice is provably among the atoms whose
+// approximate |alpha| lies within 2 eb of the maximum (key truncation and the strictness of the
+// squared comparison covered by a 2^-17 relative margin), provided no support atom can compete:
+// a support atom's FP32 alpha is the residual of the FP32 Cholesky solve, at most
+// (5 i + 4) 2^-24 ||c||_1 + max_q d_q |c_q| (backward error of Cholesky factorisation and solves,
+// rows of L of unit norm; the pivot uses 1 for G(p, p)), plus its own approximation bound.  Those
+// candidates are re-evaluated in FP32 with exactly the FP32 path's operations and the first
+// maximum among them wins, so the selection, the stop tests and the coefficients are those of
+// the FP32 Batch-OMP.  When the maximum does not stand clear of 4 eb, of the support atoms'
+// reach or of the stop threshold, or more than kMaxCand atoms are candidates, the step's alpha
+// is recomputed in FP32.
 template <int KPL, int TMAX, bool H16>
 __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
-                                           const uint16_t* __restrict__ Gh, float tol,
+                                           const uint16_t* __restrict__ Gh,
+                                           const float* __restrict__ mu_col,
                                            int64_t ldg, const float* __restrict__ a0col, int K,
                                            int T, bool emode, float e2, float xn2,
                                            int32_t* __restrict__ idx_s, float* __restrict__ coef_s,
@@ -130,6 +155,8 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
   constexpr int NG = KPL / V;
   constexpr int SPL = TMAX / 32; // support slots per lane; lane owns slots lane + 32*j
   const int lane = threadIdx.x & 31;
+  // H16: the dictionary's largest |G(k, k) - 1| (stored after the Kp column coherences)
+  const float dmax = H16 ? __ldg(mu_col + 32 * KPL) : 0.f;
   // Rows >= K of G and alpha0 are zero (every caller pads them), so the padded atoms' alpha
   // stays 0 (or NaN) and never wins a strict comparison against the first real atom: the
   // per-element passes need no k < K test.
@@ -148,8 +175,9 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
     __syncwarp();
     int ind[SPL];
     float y[SPL], c[SPL];
+    float muq[SPL];            // H16: coherence of each support column
 #pragma unroll
-    for (int j = 0; j < SPL; ++j) { ind[j] = -1; y[j] = 0.f; c[j] = 0.f; }
+    for (int j = 0; j < SPL; ++j) { ind[j] = -1; y[j] = 0.f; c[j] = 0.f; muq[j] = 0.f; }
 
     // alpha = alpha0 - G(:, I) c in FP32: one support column per step, in slot order (deeper
     // unrolling measured slower: register pressure); G's columns bypass L1 allocation -- they
@@ -210,7 +238,6 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
     float r2 = xn2;
     int i = 0;
     bool approx = false;   // al holds the FP16 update's alpha
-    float errb = 0.f;      // its error allowance per atom
     // this lane's two largest approximate |alpha| as keys, formed by the FP16 update's last pass:
     // the bits of |alpha| (positive floats order like unsigned integers) with the low five
     // mantissa bits replaced by 31 - (the element's slot in the lane), so one unsigned max tracks
@@ -239,8 +266,26 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
           const float b1 = __uint_as_float(c1 & 0x7FFFFFE0u);
           const float b2 = __uint_as_float(c2 & 0x7FFFFFE0u);
           bv = b1 * b1;
+          // the bound's inputs: ||c||_1, sum_r mu_r |c_r|, max |c_r|; the support atoms' reach
+          // (5 i + 4) 2^-24 ||c||_1 + dmax max|c| (their FP32 alpha) + 2^-9 (1 + dmax) max|c|
+          float cl1 = 0.f, w1 = 0.f, cm = 0.f;
+#pragma unroll
+          for (int j = 0; j < SPL; ++j)
+            if (lane + 32 * j < i) {
+              const float ac = fabsf(c[j]);
+              cl1 += ac;
+              w1 = fmaf(pick<SPL>(muq, j), ac, w1);
+              cm = fmaxf(cm, ac);
+            }
+          cl1 = warp_sum(cl1);
+          w1 = warp_sum(w1);
+          cm = warp_max(cm);
+          const float errb = alpha_bound(w1, cl1, i, b1);
+          const float reach = (float)(5 * i + 4) * ldexpf(cl1, -24) * 1.01f +
+                              cm * (dmax * 1.01f + ldexpf(1.f + dmax, -9));
           const float thr = b1 - 2.f * errb - ldexpf(b1, -17);
-          bool full = !(b1 > 4.f * errb) || !(b1 > 1e-6f) || !(b1 <= 3.0e38f);
+          bool full = !(b1 > 4.f * errb) || !(b1 > 1e-6f) || !(b1 <= 3.0e38f) ||
+                      !(thr > reach + errb);
           if (!full && !(b2 < thr)) {
             // near tie: every atom within 2 errb of the maximum is a candidate
             unsigned mine = 0;
@@ -342,7 +387,11 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
         }
       }
       if (lane == 0) L[lidx<TMAX>(i, i)] = 1.f / Lii;   // the solves multiply by 1 / L_ii
-      if (lane == (i & 31)) { put<SPL>(ind, i >> 5, p); put<SPL>(y, i >> 5, ynew); }
+      if (lane == (i & 31)) {
+        put<SPL>(ind, i >> 5, p);
+        put<SPL>(y, i >> 5, ynew);
+        if constexpr (H16) put<SPL>(muq, i >> 5, __ldg(mu_col + p));
+      }
       ++i;
       __syncwarp();
 
@@ -433,7 +482,6 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
               hk2 = max(hk2, min(hk1, key));
               hk1 = max(hk1, key);
             }
-          errb = tol * cl1;
           approx = true;
         } else {
           exact_alpha(i);
@@ -471,15 +519,10 @@ __host__ __device__ constexpr int warp_smem_floats_for(int T) {
   return l_floats_for<TMAX>(T) + 32 * KPL + kMaxCand;
 }
 
-// Error allowance factor of the FP16 update from the coherence mu (as float bits, >= 0).
-__device__ __forceinline__ float h16_tolerance(const unsigned* mu_bits) {
-  return ldexpf(__uint_as_float(*mu_bits), -12) + ldexpf(1.f, -18);
-}
-
 template <int KPL, int TMAX, bool H16, bool QUEUE>
 __global__ void __launch_bounds__(kOmpWarps * 32, (TMAX <= 32 ? 3 : 2))
 omp_kernel(const float* __restrict__ G, const uint16_t* __restrict__ Gh,
-           const unsigned* __restrict__ mu_bits, int64_t ldg, const float* __restrict__ A0,
+           const float* __restrict__ mu_col, int64_t ldg, const float* __restrict__ A0,
            int64_t lda, int K, int64_t N, int T, const float* __restrict__ xnorm2,
            const float* __restrict__ eps2, int32_t* __restrict__ idx_out,
            float* __restrict__ coef_out, int32_t* __restrict__ nnz_out, int* __restrict__ dev_err,
@@ -490,7 +533,6 @@ omp_kernel(const float* __restrict__ G, const uint16_t* __restrict__ Gh,
   float* L = smem + (size_t)wib * warp_smem_floats_for<KPL, TMAX>(T);   // Cholesky factor
   float* a0s = L + l_floats_for<TMAX>(T);                                // alpha0 column
   int* cand = reinterpret_cast<int*>(a0s + 32 * KPL);
-  const float tol = H16 ? h16_tolerance(mu_bits) : 0.f;
   bool numeric_bad = false;
   const bool emode = eps2 != nullptr;
   if constexpr (QUEUE) {
@@ -504,7 +546,7 @@ omp_kernel(const float* __restrict__ G, const uint16_t* __restrict__ Gh,
       if (s0 >= N) break;
       const int64_t s1 = min(N, s0 + kOmpClaim);
       for (int64_t s = s0; s < s1; ++s)
-        omp_signal<KPL, TMAX, H16>(G, Gh, tol, ldg, A0 + s * lda, K, T, emode,
+        omp_signal<KPL, TMAX, H16>(G, Gh, mu_col, ldg, A0 + s * lda, K, T, emode,
                                    emode ? eps2[s] : 0.f, emode ? xnorm2[s] : 0.f,
                                    idx_out + s * T, coef_out + s * T, nnz_out + s, L, a0s, cand,
                                    numeric_bad);
@@ -512,7 +554,7 @@ omp_kernel(const float* __restrict__ G, const uint16_t* __restrict__ Gh,
   } else {
     const int64_t warps_total = (int64_t)gridDim.x * kOmpWarps;
     for (int64_t s = (int64_t)blockIdx.x * kOmpWarps + wib; s < N; s += warps_total)
-      omp_signal<KPL, TMAX, H16>(G, Gh, tol, ldg, A0 + s * lda, K, T, emode,
+      omp_signal<KPL, TMAX, H16>(G, Gh, mu_col, ldg, A0 + s * lda, K, T, emode,
                                  emode ? eps2[s] : 0.f, emode ? xnorm2[s] : 0.f, idx_out + s * T,
                                  coef_out + s * T, nnz_out + s, L, a0s, cand, numeric_bad);
   }
@@ -564,8 +606,8 @@ omp_batched_kernel(const OmpJob* __restrict__ jobs, int njobs, int64_t total_chu
       float* co = jb.coef + s * jb.T;
       switch (jb.kpl) {
 #define KSVD_BATCHED_SIGNAL(KPL)                                                              \
-  omp_signal<KPL, TMAX, false>(jb.G, nullptr, 0.f, jb.ldg, a0, jb.K, jb.T, emode, e2, xn2, io, \
-                               co, jb.nnz + s, L, a0s, cand, numeric_bad)
+  omp_signal<KPL, TMAX, false>(jb.G, nullptr, nullptr, jb.ldg, a0, jb.K, jb.T, emode, e2, xn2, \
+                               io, co, jb.nnz + s, L, a0s, cand, numeric_bad)
         case 4: KSVD_BATCHED_SIGNAL(4); break;
         case 8: KSVD_BATCHED_SIGNAL(8); break;
         case 16: KSVD_BATCHED_SIGNAL(16); break;
@@ -578,7 +620,7 @@ omp_batched_kernel(const OmpJob* __restrict__ jobs, int njobs, int64_t total_chu
 }
 
 template <int KPL, int TMAX, bool H16>
-cudaError_t launch_omp_t(const float* G, const uint16_t* Gh, const unsigned* mu, int64_t ldg,
+cudaError_t launch_omp_t(const float* G, const uint16_t* Gh, const float* mu, int64_t ldg,
                          const float* A0, int64_t lda, int K, int64_t N, int T,
                          const float* xnorm2, const float* eps2, int32_t* idx, float* coef,
                          int32_t* nnz, int* dev_err, int grid_mult, unsigned long long* queue,
@@ -649,42 +691,56 @@ int omp_padded_k(int K) {
   return K <= 128 ? 128 : K <= 256 ? 256 : K <= 512 ? 512 : 1024;
 }
 
-// FP16 copy of G and the coherence mu = max_{i != j < K} |G(i, j)| (float bits, zeroed by the
-// caller), for the mixed path's alpha update.
-__global__ void gram_half_kernel(const float* __restrict__ G, int64_t ldg, int K, int64_t cols,
-                                 uint16_t* __restrict__ Gh, unsigned* __restrict__ mu_bits) {
-  const int64_t total = ldg * cols;
-  float mx = 0.f;
+// FP16 copy of G, elementwise.
+__global__ void gram_half_kernel(const float* __restrict__ G, int64_t total,
+                                 uint16_t* __restrict__ Gh) {
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const float g = G[e];
-    Gh[e] = __half_as_ushort(__float2half_rn(g));
-    const int64_t col = e / ldg, row = e - col * ldg;
-    if (row < K && col < K && row != col) mx = fmaxf(mx, fabsf(g));
-  }
-  mx = warp_max(mx);
-  if ((threadIdx.x & 31) == 0 && mx > 0.f) atomicMax(mu_bits, __float_as_uint(mx));
+       e += (int64_t)gridDim.x * blockDim.x)
+    Gh[e] = __half_as_ushort(__float2half_rn(G[e]));
 }
 
-cudaError_t launch_gram_half(const float* G, int64_t ldg, int K, uint16_t* Gh, unsigned* mu,
+// Per-column coherence mu_col[c] = max_{k != c, k < K} |G(k, c)| (column c of the stored matrix,
+// as the FP32 alpha update reads it), zero for padding columns; one warp per column.  Block 0
+// also writes mu_col[kp] = max_{k < K} |G(k, k) - 1| (G's unit diagonal up to rounding).
+__global__ void column_coherence_kernel(const float* __restrict__ G, int64_t ldg, int K, int kp,
+                                        float* __restrict__ mu_col) {
+  const int lane = threadIdx.x & 31;
+  if (blockIdx.x == 0 && threadIdx.x < 32) {
+    float dm = 0.f;
+    for (int k = lane; k < K; k += 32) dm = fmaxf(dm, fabsf(G[(int64_t)k * ldg + k] - 1.f));
+    dm = warp_max(dm);
+    if (lane == 0) mu_col[kp] = dm;
+  }
+  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (c >= kp) return;
+  float mx = 0.f;
+  if (c < K)
+    for (int k = lane; k < K; k += 32)
+      if (k != c) mx = fmaxf(mx, fabsf(G[(int64_t)c * ldg + k]));
+  mx = warp_max(mx);
+  if (lane == 0) mu_col[c] = mx;
+}
+
+cudaError_t launch_gram_half(const float* G, int64_t ldg, int K, uint16_t* Gh, float* mu_col,
                              cudaStream_t st) {
   const int kp = omp_padded_k(K);
   if (K < 1 || K > kMaxK || ldg < kp) return cudaErrorInvalidValue;
-  cudaError_t e = cudaMemsetAsync(mu, 0, sizeof(unsigned), st);
-  if (e != cudaSuccess) return e;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int64_t need = (ldg * kp + 255) / 256;
-  const unsigned blocks = (unsigned)std::min<int64_t>(need, (int64_t)sms * 8);
-  gram_half_kernel<<<blocks, 256, 0, st>>>(G, ldg, K, kp, Gh, mu);
+  const int64_t total = ldg * kp;
+  const unsigned blocks = (unsigned)std::min<int64_t>((total + 255) / 256, (int64_t)sms * 8);
+  gram_half_kernel<<<blocks, 256, 0, st>>>(G, total, Gh);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  column_coherence_kernel<<<(kp + 7) / 8, 256, 0, st>>>(G, ldg, K, kp, mu_col);
   return cudaGetLastError();
 }
 
 cudaError_t launch_omp(const float* G, int64_t ldg, const float* A0, int64_t lda, int K,
                        int64_t N, int T, const float* xnorm2, const float* eps2, int32_t* idx,
                        float* coef, int32_t* nnz, int* dev_err, cudaStream_t st, int grid_mult,
-                       const uint16_t* Gh, const unsigned* mu, unsigned long long* queue) {
+                       const uint16_t* Gh, const float* mu, unsigned long long* queue) {
   if (N <= 0) return cudaSuccess;
   if (K < 1 || K > kMaxK || T < 1 || T > kMaxT) return cudaErrorInvalidValue;
   const int kp = omp_padded_k(K);   // the lanes touch rows [0, kp) of every column

@@ -108,9 +108,9 @@ def _coding_inputs(case):
                                   "scale-up", "scale-down", "t32", "eps"])
 def test_fp16_alpha_update_selects_like_fp32(cuda, case):
     """The mixed path's Batch-OMP forms alpha from an FP16 copy of G and re-evaluates every atom
-    within its error allowance of the maximum in FP32 with the FP32 path's operations.  Given the
-    same G and alpha0 its supports, coefficients and support sizes are bit-identical to the FP32
-    Batch-OMP's: on incoherent dictionaries (few near ties), on nearly duplicated atoms (many
+    within its rigorous error bound of the maximum in FP32 with the FP32 path's operations.  Given
+    the same G and alpha0 its supports, coefficients and support sizes are bit-identical to the
+    FP32 Batch-OMP's: on incoherent dictionaries (few near ties), on nearly duplicated atoms (many
     candidates: the whole-alpha FP32 fallback), on noiseless signals (the stop tests at
     exhaustion), at K not a multiple of 128 (also K <= 128: four rows per lane and group), with
     signals scaled by 1e4 and 1e-4 (the coefficients' power-of-two scaling into FP16 range), at
@@ -138,3 +138,31 @@ def test_fp16_alpha_update_selects_like_fp32(cuda, case):
     assert torch.equal(na, nb)
     assert torch.equal(ia, ib)
     assert torch.equal(ca, cb)
+
+
+def test_fp16_update_identical_at_full_cfg2_size(cuda):
+    """The FP16 alpha update against the FP32 kernel on the whole cfg2 workload (n=256, K=1024,
+    1,000,000 signals, T=16) given the same G and alpha0: identical supports, coefficients and
+    support sizes on every signal (the error bound is rigorous, so no mismatch is allowed)."""
+    import torch
+
+    from ksvd_gb300 import Handle, datagen
+
+    c = datagen.CONFIGS["cfg2"]
+    p = datagen.make_problem("cfg2", device="cuda")
+    D = p["D"] / p["D"].norm(dim=1, keepdim=True)
+    G = (D @ D.T).contiguous()
+    A0 = (p["X"] @ D.T).contiguous()
+    del p
+    outs = []
+    for prec in ("fp32", "mixed"):
+        h = Handle(c.n, c.K, c.T, precision=prec)
+        if prec == "mixed":
+            h.tuning = dict(h.tuning, omp_fp16=1)
+        outs.append(h.omp_gram(G, A0))
+        h.synchronize()
+        h.close()
+    (ia, ca, na), (ib, cb, nb) = outs
+    assert A0.shape[0] == 1_000_000
+    bad = int(((ia != ib).any(1) | (ca != cb).any(1) | (na != nb)).sum())
+    assert bad == 0, "%d of %d signals differ" % (bad, A0.shape[0])
