@@ -138,7 +138,12 @@ def stage_flops(cfg, N, stage):
 # the source changes, no entry matches and the line reports traffic as null instead of a stale
 # figure.
 KERNEL_SOURCES = {"omp": ("omp.cu",)}
-MEASURED_OMP = {}   # (n, K, T, precision, fingerprint) -> (bytes per signal, L2 %, issue %)
+# (n, K, T, precision, fingerprint) -> (bytes per signal, L2 %, issue %): omp_kernel<32, 32, H16, 1>
+# at 100,000 signals, dram__bytes_read.sum + dram__bytes_write.sum per signal
+MEASURED_OMP = {
+    (256, 1024, 16, "mixed", "131851db534dfae7"): ((415998976 + 7024896) / 100_000, 44.93, 67.97),
+    (256, 1024, 16, "fp32", "131851db534dfae7"): ((413822464 + 7335168) / 100_000, 75.32, 52.30),
+}
 
 
 def source_fingerprint(stage):
@@ -154,6 +159,20 @@ def source_fingerprint(stage):
 
 # FP32 CUDA-core peak (nominal): 152 SMs x 128 FMA lanes x 2 FLOP x 2.07 GHz.
 FP32_SIMT_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
+
+
+def cpu_time_at(N, Ns, ts, Nl, tl):
+    """Seconds of one CPU iteration at N signals from timings at two sample sizes: the affine
+    model t = a + b n through (Ns, ts) and (Nl, tl) -- a holds the per-iteration work that does
+    not grow with the signals (the K-dependent parts of the sweep and clearDict); linear in N
+    from the larger sample when only one size was timed or the fit is not increasing."""
+    if tl is None or Nl <= Ns:
+        return ts * N / Ns
+    b = (tl - ts) / (Nl - Ns)
+    a = ts - b * Ns
+    if b <= 0 or a < 0:
+        return tl * N / Nl
+    return a + b * N
 
 
 def max_over_ranks(x, dist, device):
@@ -220,16 +239,19 @@ def run_reference(args, cfg):
         if step >= args.warmup:
             times.append(dt)
     t = statistics.median(times)
-    value = 1.0 / (t * cfg.N / Ns)          # iterations/s at the full N, linear in N
     lin = None
+    tl = None
     if Nl > Ns:
         perm = rng.permutation(cfg.K).astype(np.int32)[None, :]
         t0 = time.perf_counter()
         oracle.ksvd(XL, DL.copy(order="F"), cfg.T, 1, perm)
         tl = time.perf_counter() - t0
-        lin = {"signals": [Ns, Nl], "s_per_signal": [t / Ns, tl / Nl],
+    value = 1.0 / cpu_time_at(cfg.N, Ns, t, Nl, tl)   # iterations/s at the full N
+    if tl is not None:
+        lin = {"signals": [Ns, Nl], "seconds": [t, tl], "s_per_signal": [t / Ns, tl / Nl],
                "ratio_large_over_small": (tl / Nl) / (t / Ns),
-               "value_from_large_sample": 1.0 / (tl * cfg.N / Nl)}
+               "value_linear_from_small": 1.0 / (t * cfg.N / Ns),
+               "value_linear_from_large": 1.0 / (tl * cfg.N / Nl)}
     line = {
         "impl": "reference", "metric": "ksvd_iters_per_s", "value": value, "unit": "iter/s",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -239,11 +261,11 @@ def run_reference(args, cfg):
                    % (cfg.name, cfg.n, cfg.K, cfg.N, cfg.T), "n": cfg.n, "K": cfg.K,
                    "N": cfg.N, "T": cfg.T},
         "cpu_baseline": {"value": value, "unit": "iter/s", "cores": threads, "kind": "port",
-                         "sample": "%d of %d signals per step (%.2f s each), median of %d steps, "
-                         "scaled by N; linearity check: one iteration on %d signals costs %s the "
-                         "per-signal time of the %d-signal steps"
+                         "sample": "%d of %d signals per step (%.2f s each, median of %d steps) "
+                         "and one iteration on %d signals (%s); the full-N time from the affine "
+                         "fit t = a + b N through the two sizes"
                          % (Ns, cfg.N, t, args.steps, Nl,
-                            "%.3fx" % lin["ratio_large_over_small"] if lin else "(n/a)", Ns),
+                            "%.2f s" % tl if tl is not None else "n/a"),
                          "linearity": lin},
         "sample_s_per_step": t,
         "e2e": {"value": value, "unit": "iter/s", "h2d_bytes_per_step": 0,
@@ -280,15 +302,17 @@ def cpu_baseline(cfg, sample, reps=1, check_iters=3, check_signals=20000):
         t0 = time.perf_counter()
         oracle.ksvd(p["X"], p["D"], cfg.T, 1, perm)
         tl = time.perf_counter() - t0
-    base = {"value": 1.0 / (t * cfg.N / Ns), "unit": "iter/s", "cores": oracle.num_threads(),
-            "kind": "port",
-            "sample": "one K-SVD iteration on %d of %d signals (%.2f s), scaled by N%s" %
+    base = {"value": 1.0 / cpu_time_at(cfg.N, Ns, t, Nl, tl), "unit": "iter/s",
+            "cores": oracle.num_threads(), "kind": "port",
+            "sample": "one K-SVD iteration on %d of %d signals (%.2f s)%s; the full-N time from "
+                      "the affine fit t = a + b N through the two sizes" %
                       (Ns, cfg.N, t, "" if tl is None else
-                       "; on %d signals %.2f s (%.3fx the per-signal time)"
-                       % (Nl, tl, (tl / Nl) / (t / Ns)))}
+                       " and one on %d signals (%.2f s)" % (Nl, tl))}
     if tl is not None:
-        base["linearity"] = {"signals": [Ns, Nl], "s_per_signal": [t / Ns, tl / Nl],
-                             "ratio_large_over_small": (tl / Nl) / (t / Ns)}
+        base["linearity"] = {"signals": [Ns, Nl], "seconds": [t, tl],
+                             "s_per_signal": [t / Ns, tl / Nl],
+                             "ratio_large_over_small": (tl / Nl) / (t / Ns),
+                             "value_linear_from_small": 1.0 / (t * cfg.N / Ns)}
     check = None
     if check_iters > 0:
         rng = np.random.default_rng(1)

@@ -164,6 +164,8 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_constant
       if (it >= STAGES && !mbar_wait(&empty[s], (use - 1) & 1)) {
         atomicOr(P.dev_err, kDevErrTimeout);
         *(volatile int*)abort_flag = 1;
+        // before the CTA releases its shared memory: the loads still in flight land (bounded)
+        for (int gg = it - STAGES; gg < it; ++gg) mbar_wait(&full[gg % STAGES], (gg / STAGES) & 1);
         break;
       }
       const int pass = it / P.nk, kc = it % P.nk;
@@ -195,8 +197,10 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA_hi, const __grid_constant
         umma_bf16(tmem, ad + 2 * j, bd + 2 * j, (it > 0 || j > 0) ? 1u : 0u);
       umma_commit(&empty[s]);
     }
-    if (ok) umma_commit(done);
-    else *(volatile int*)abort_flag = 1;
+    if (!ok) *(volatile int*)abort_flag = 1;
+    // done tracks every MMA issued so far: on an abort too, the epilogue's wait on it keeps
+    // TMEM allocated until they have finished
+    umma_commit(done);
   }
   __syncwarp();
 
@@ -270,11 +274,13 @@ gemm_tc_persistent_kernel(const __grid_constant__ CUtensorMap tmA_hi,
   uint64_t* empty = full + PSTAGES;
   uint64_t* tfull = empty + PSTAGES;
   uint64_t* tempty = tfull + 2;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + 2);
+  uint64_t* drain = tempty + 2;   // abort: completion of every MMA already issued
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
   int* abort_flag = reinterpret_cast<int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
+    mbar_init(drain, 1);
     for (int s = 0; s < PSTAGES; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
@@ -316,6 +322,9 @@ gemm_tc_persistent_kernel(const __grid_constant__ CUtensorMap tmA_hi,
             if (!*(volatile int*)abort_flag) atomicOr(P.dev_err, kDevErrTimeout);
             *(volatile int*)abort_flag = 1;
             ok = false;
+            // before the CTA releases its shared memory: the loads still in flight land
+            for (int64_t gg = g >= PSTAGES ? g - PSTAGES : 0; gg < g; ++gg)
+              mbar_wait(&full[gg % PSTAGES], (uint32_t)(gg / PSTAGES) & 1);
             break;
           }
           const int pass = it / P.nk, kc = it % P.nk;
@@ -364,7 +373,12 @@ gemm_tc_persistent_kernel(const __grid_constant__ CUtensorMap tmA_hi,
         }
         if (ok) umma_commit(&tfull[b]);
       }
-      if (!ok) *(volatile int*)abort_flag = 1;
+      if (!ok) {
+        *(volatile int*)abort_flag = 1;
+        // the MMAs already issued finish before TMEM is released (bounded wait)
+        umma_commit(drain);
+        mbar_wait(drain, 0);
+      }
     }
   } else {
     // ---- epilogue warps 2..5: TMEM lanes (atoms m0 + 32 * (warp % 4) + lane)

@@ -77,3 +77,17 @@ def coef_by_atom(idx, coef, nnz, K):
         m = t < nnz
         out[np.nonzero(m)[0], idx[m, t]] = coef[m, t]
     return out
+
+
+def touched_atoms(idx_a, nnz_a, idx_b, nnz_b, K):
+    """(signals whose support sets differ, boolean mask of the atoms in either of their supports)."""
+    T = idx_a.shape[1]
+    ar = np.arange(T)[None, :]
+    sa = np.sort(np.where(ar < nnz_a[:, None], idx_a, -1), 1)
+    sb = np.sort(np.where(ar < nnz_b[:, None], idx_b, -1), 1)
+    flipped = np.nonzero(np.any(sa != sb, 1) | (nnz_a != nnz_b))[0]
+    touched = np.zeros(K, bool)
+    for s in flipped:
+        touched[sa[s][sa[s] >= 0]] = True
+        touched[sb[s][sb[s] >= 0]] = True
+    return flipped, touched

@@ -7,7 +7,7 @@ seeded inputs.  Tolerances (FP32 GPU vs FP64 oracle):
 import numpy as np
 import pytest
 
-from conftest import coef_by_atom, rel_rmse, support_match_vec
+from conftest import coef_by_atom, rel_rmse, support_match_vec, touched_atoms
 
 pytestmark = pytest.mark.gpu
 
@@ -231,8 +231,10 @@ def test_stage_order_is_enforced(cuda):
 @pytest.mark.parametrize("cfg,N", [("cfg0", 4000), ("ref", 3600), ("cfg2", 20000)])
 def test_iterate_matches_oracle(oracle_mod, cuda, cfg, N):
     """Whole iterations through ksvd_iterate.  After one iteration: supports (>= 99.9%) and the
-    dictionary (relative RMSE <= 1e-3 -- one support chosen differently at a near-tie moves the
-    atoms it touches) against the FP64 oracle.  Over three iterations: the RMSE of every
+    dictionary against the FP64 oracle -- relative RMSE <= 1e-4 when every support agrees; when a
+    near tie codes a signal differently, <= 5e-3 over all atoms (the atoms of both supports move
+    by ~1/(signals per atom)) and <= 5e-4 over the atoms no differently coded signal touches
+    (they move through the sweep's coupling only).  Over three iterations: the RMSE of every
     iteration within 1e-3.  Later supports are not compared: K-SVD amplifies a single near-tie
     flip from iteration to iteration in any two implementations that round differently."""
     from ksvd_gb300 import Handle, datagen, random_permutation
@@ -249,9 +251,22 @@ def test_iterate_matches_oracle(oracle_mod, cuda, cfg, N):
     match = support_match_vec(idx.cpu().numpy(), nnz.cpu().numpy(), ri, rn)
     assert match >= SUPPORT_MIN
     # with identical supports the sweep agrees to rounding; each signal coded differently moves
-    # the atoms it touches by ~1/(signals per atom), and the sweep couples later atoms to them
-    flips = round((1.0 - match) * N)
-    assert rel_rmse(from_dev(Dd), Dr) <= (REL_TOL if flips == 0 else 5e-3)
+    # the atoms of both of its supports by ~1/(signals per atom): those atoms are held to 5e-3,
+    # every other atom to 1e-4
+    Dg = from_dev(Dd)
+    flipped, touched = touched_atoms(idx.cpu().numpy(), nnz.cpu().numpy(), ri, rn, c.K)
+    e_all = rel_rmse(Dg, Dr)
+    e_unt = rel_rmse(Dg[:, ~touched], Dr[:, ~touched]) if (~touched).any() else 0.0
+    print("%s: %d flipped signals, %d touched atoms, dictionary rel RMSE %.2e (untouched atoms "
+          "%.2e)" % (cfg, len(flipped), touched.sum(), e_all, e_unt))
+    if len(flipped) == 0:
+        assert e_all <= REL_TOL
+    else:
+        # the sweep couples every later atom to the moved ones through the residuals of the
+        # signals they share, so the untouched atoms move too, an order of magnitude less
+        # (measured at cfg2: one flipped signal, 20 touched atoms, 2.2e-4 elsewhere)
+        assert e_unt <= 5e-4
+        assert e_all <= 5e-3
     np.testing.assert_allclose(rmse, rr, rtol=REL_TOL)
     Dr3, _, _, _, rr3 = oracle_mod.ksvd(X64, D64, c.T, 3, perms)
     Dd = to_dev(D, cuda)
