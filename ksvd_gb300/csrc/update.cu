@@ -298,6 +298,33 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
   return v;
 }
 
+// Warp sum of M values per lane (M = 1, 2 or 4) in one shuffle tree: the first log2(M) levels
+// exchange halves of the value set, so M values cost M - 1 + 5 - log2(M) shuffles instead of 5 M.
+// Every lane returns the full sum of value (lane >> (5 - log2 M)).
+template <int M>
+__device__ __forceinline__ float warp_sum_multi(const float (&v)[M], int lane) {
+  float b;
+  if constexpr (M == 4) {
+    const bool u16 = lane & 16, u8 = lane & 8;
+    const float a0 = (u16 ? v[2] : v[0]) + __shfl_xor_sync(KSVD_FULL_MASK, u16 ? v[0] : v[2], 16);
+    const float a1 = (u16 ? v[3] : v[1]) + __shfl_xor_sync(KSVD_FULL_MASK, u16 ? v[1] : v[3], 16);
+    b = (u8 ? a1 : a0) + __shfl_xor_sync(KSVD_FULL_MASK, u8 ? a0 : a1, 8);
+    b += __shfl_xor_sync(KSVD_FULL_MASK, b, 4);
+  } else if constexpr (M == 2) {
+    const bool u16 = lane & 16;
+    b = (u16 ? v[1] : v[0]) + __shfl_xor_sync(KSVD_FULL_MASK, u16 ? v[0] : v[1], 16);
+    b += __shfl_xor_sync(KSVD_FULL_MASK, b, 8);
+    b += __shfl_xor_sync(KSVD_FULL_MASK, b, 4);
+  } else {
+    b = v[0];
+#pragma unroll
+    for (int o = 16; o >= 4; o >>= 1) b += __shfl_xor_sync(KSVD_FULL_MASK, b, o);
+  }
+  b += __shfl_xor_sync(KSVD_FULL_MASK, b, 2);
+  b += __shfl_xor_sync(KSVD_FULL_MASK, b, 1);
+  return b;
+}
+
 // Brings every 128-byte line of [p, p + bytes) into L2: one L2-only load per line whose value is
 // never used (nothing waits for it).  Measured better than prefetch.global.L2, which the memory
 // system may drop, and than bulk prefetches, which queue on the SM's single TMA unit.
@@ -580,6 +607,9 @@ struct Sweep {
     const int64_t per = (cnt + nctas - 1) / nctas;
     const int64_t qa = q0 + min(cnt, (int64_t)c * per), qb = q0 + min(cnt, (int64_t)(c + 1) * per);
     const int32_t* st = stage + buf * kStageCap;
+    // e / T as a multiply and shift: exact for e < 2^31, T <= 64 (the error e T / 2^40 < 2^-9
+    // stays below the 1/T gap to the next integer)
+    const uint64_t magic = ((1ull << 40) + (uint64_t)T - 1) / (uint64_t)T;
     int my_use = 0;
     for (;;) {
       int bidx = 0;
@@ -593,7 +623,7 @@ struct Sweep {
       for (int b = 0; b < EB; ++b) {
         const int64_t q = qs + b;
         e[b] = b < ne ? (q - qa < kStageCap ? (int64_t)st[q - qa] : (int64_t)A.list[q]) : 0;
-        s[b] = e[b] / T;
+        s[b] = (int64_t)(((uint64_t)e[b] * magic) >> 40);
       }
       // the signal, its whole code row and its support size, all in one round of loads
       float xv[EB][NPL];
@@ -629,7 +659,8 @@ struct Sweep {
           cf[b][u] = ok ? cf[b][u] : 0.f;
         }
       }
-      float ax[EB], gs[EB];
+      // this lane's part of a.x_s - Gamma(:,s).(a'D) per entry, summed over the warp in one tree
+      float dpart[EB];
 #pragma unroll
       for (int b = 0; b < EB; ++b) {
         float acc = 0.f;
@@ -638,28 +669,33 @@ struct Sweep {
           const int r = lane + 32 * i;
           if (r < n) acc = fmaf(a_s[r], xv[b][i], acc);
         }
-        ax[b] = acc;
-        float g = 0.f;
 #pragma unroll
         for (int u = 0; u < 2; ++u)
-          if (ix[b][u] >= 0) g = fmaf(cf[b][u], aD_s[ix[b][u]], g);
-        gs[b] = g;
+          if (ix[b][u] >= 0) acc = fmaf(-cf[b][u], aD_s[ix[b][u]], acc);
+        dpart[b] = acc;
       }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1)
-#pragma unroll
-        for (int b = 0; b < EB; ++b) {
-          ax[b] += __shfl_xor_sync(KSVD_FULL_MASK, ax[b], o);
-          gs[b] += __shfl_xor_sync(KSVD_FULL_MASK, gs[b], o);
-        }
+      const float dsum = warp_sum_multi<EB>(dpart, lane);   // entry lane >> (5 - log2 EB)
+      constexpr int SH = EB == 4 ? 3 : (EB == 2 ? 4 : 5);
+      float gold[EB];
 #pragma unroll
       for (int b = 0; b < EB; ++b) {
         // gamma_j(s) is slot e % T of the code row already in registers
         const int ts = (int)(e[b] - s[b] * T);
-        const float gold =
-            __shfl_sync(KSVD_FULL_MASK, (ts >> 5) == 0 ? cf[b][0] : cf[b][1], ts & 31);
+        gold[b] = __shfl_sync(KSVD_FULL_MASK, (ts >> 5) == 0 ? cf[b][0] : cf[b][1], ts & 31);
+      }
+      float gmine = 0.f;
+      {
+        const int mb = lane >> SH;
+        float go = gold[0];
+#pragma unroll
+        for (int b = 1; b < EB; ++b)
+          if (mb == b) go = gold[b];
+        gmine = (dsum + aDj * go) / anorm;
+      }
+#pragma unroll
+      for (int b = 0; b < EB; ++b) {
+        const float g = __shfl_sync(KSVD_FULL_MASK, gmine, (b << SH) & 31);
         if (b >= ne) continue;
-        const float g = (ax[b] - gs[b] + aDj * gold) / anorm;
 #pragma unroll
         for (int u = 0; u < 2; ++u)
           if (ix[b][u] >= 0 && ix[b][u] != j) atomicAdd(cpart + ix[b][u], g * cf[b][u]);
