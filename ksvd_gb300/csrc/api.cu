@@ -342,7 +342,7 @@ ksvd_status dtx_padded_range(ksvd_handle* h, const float* Dp, const float* X, in
 
 ksvd_status run_omp(ksvd_handle* h, const float* G, const float* A0, int64_t N,
                     const float* xnorm2, const float* eps2, int32_t* idx, float* coef,
-                    int32_t* nnz) {
+                    int32_t* nnz, bool make_gh = true) {
   int* de = nullptr;
   KSVD_TRY(ensure(h, B_DEVERR, 1, &de));
   // mixed path: the alpha update reads an FP16 copy of G (made here, G may have changed since
@@ -359,7 +359,7 @@ ksvd_status run_omp(ksvd_handle* h, const float* G, const float* A0, int64_t N,
   unsigned long long* q = nullptr;     // grid_mult 0: signals claimed from a work queue
   if (h->omp_grid_mult == 0) KSVD_TRY(ensure(h, B_OMPQ, 1, &q));
   StageScope sc(h, KSVD_STAGE_OMP);
-  if (gh) KSVD_CK(h, launch_gram_half(G, h->Kp, h->p.K, gh, mu, h->stream));
+  if (gh && make_gh) KSVD_CK(h, launch_gram_half(G, h->Kp, h->p.K, gh, mu, h->stream));
   KSVD_CK(h, launch_omp(G, h->Kp, A0, h->Kp, h->p.K, N, h->p.T, xnorm2, eps2, idx, coef, nnz, de,
                         h->stream, h->omp_grid_mult, gh, mu, q));
   return KSVD_OK;
@@ -1277,7 +1277,7 @@ ksvd_status iteration_body(ksvd_handle* h, float* Dp, float* G, float* A0, const
                                     const_cast<float*>(h->it_xn2) + s0, h->stream));
       KSVD_TRY(run_omp(h, G, A0 + s0 * h->Kp, s1 - s0, h->it_eps2 ? h->it_xn2 + s0 : nullptr,
                        h->it_eps2 ? h->it_eps2 + s0 : nullptr, idx + s0 * h->p.T,
-                       coef + s0 * h->p.T, nnz + s0));
+                       coef + s0 * h->p.T, nnz + s0, c == 0));   // G's FP16 copy: once
     }
     if (mixed(h)) { h->xsplit_src = X; h->xsplit_N = N; }   // every chunk's split is made
   } else {
@@ -1610,7 +1610,21 @@ static ksvd_status iterate_host_body(ksvd_handle* h, float* D, const float* X, i
   // X in chunks on a copy stream (after the work already queued on the handle's stream), so the
   // first iteration's D'X and Batch-OMP overlap the rest of the transfer
   auto& in = h->inflow;
-  const int nch = (int)std::min<int64_t>(ksvd_handle::kMaxInflow, std::max<int64_t>(1, N / 65536));
+  // Chunks growing fourfold from 65,536 signals: the first lands after a short wait, and each
+  // later one lands while Batch-OMP codes the one before (a signal's coding takes ~4x its copy),
+  // with few launches -- every Batch-OMP launch ends in a tail where SMs idle.
+  int64_t cb[ksvd_handle::kMaxInflow + 1];
+  int nch = 0;
+  cb[0] = 0;
+  for (int64_t sz = 65536; cb[nch] < N && nch < ksvd_handle::kMaxInflow; sz *= 4) {
+    cb[nch + 1] = (nch + 1 == ksvd_handle::kMaxInflow || cb[nch] + sz >= N) ? N : cb[nch] + sz;
+    ++nch;
+  }
+  if (nch >= 2 && N - cb[nch - 1] < 65536) {   // no tiny last chunk: fold it into the one before
+    cb[nch - 1] = N;
+    --nch;
+    cb[nch] = N;
+  }
   if (iters >= 1 && nch >= 2) {
     if (!in.cstream) {
       KSVD_CK(h, cudaStreamCreateWithFlags(&in.cstream, cudaStreamNonBlocking));
@@ -1619,7 +1633,7 @@ static ksvd_status iterate_host_body(ksvd_handle* h, float* D, const float* X, i
     KSVD_CK(h, cudaEventRecord(in.ev[0], h->stream));
     KSVD_CK(h, cudaStreamWaitEvent(in.cstream, in.ev[0], 0));
     in.nchunks = nch;
-    for (int c = 0; c <= nch; ++c) in.bounds[c] = N * c / nch;
+    for (int c = 0; c <= nch; ++c) in.bounds[c] = cb[c];
     for (int c = 0; c < nch; ++c) {
       const int64_t s0 = in.bounds[c], s1 = in.bounds[c + 1];
       KSVD_CK(h, cudaMemcpyAsync(dX + s0 * n, X + s0 * n, sizeof(float) * (size_t)n * (s1 - s0),
