@@ -29,6 +29,16 @@ constexpr int kSweepThreads = 512;
 constexpr int kStageCap = 2048;   // list entries of the next atom staged per CTA (x2 buffers)
 constexpr unsigned kBarrierSpinLimit = 1u << 24;   // x >= 64 ns sleeps: > 1 s before giving up
 
+// e / T for list entries e = signal * T + slot as a multiply and shift (magic = ceil(2^40 / T)):
+// exact for 0 <= e < 2^31 and 1 <= T <= 64, the error e T / 2^40 < 2^-9 staying below the 1/T
+// gap to the next integer.  The callers keep N * T < 2^31.
+__host__ __device__ inline uint64_t div_t_magic(int T) {
+  return ((1ull << 40) + (uint64_t)T - 1) / (uint64_t)T;
+}
+__device__ __forceinline__ int64_t div_t(int64_t e, uint64_t magic) {
+  return (int64_t)(((uint64_t)e * magic) >> 40);
+}
+
 // ---- 1. atom lists --------------------------------------------------------------------------
 
 __global__ void list_count_kernel(const int32_t* __restrict__ idx, const int32_t* __restrict__ nnz,
@@ -42,8 +52,9 @@ __global__ void list_count_kernel(const int32_t* __restrict__ idx, const int32_t
   const int64_t s1 = min(N, s0 + kSigPerBlock);
   const int64_t e0 = s0 * T, e1 = s1 * T;
   bool bad = false;
+  const uint64_t magic = div_t_magic(T);
   for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-    const int64_t s = e / T;
+    const int64_t s = div_t(e, magic);
     const int t = (int)(e - s * T);
     if (t < nnz[s]) {
       const int a = idx[e];
@@ -124,11 +135,12 @@ __global__ void list_fill_kernel(const int32_t* __restrict__ idx, const int32_t*
   const int64_t s1 = min(N, s0 + kSigPerBlock);
   const int64_t e0 = s0 * T, e1 = s1 * T;
   const unsigned lt_mask = (1u << lane) - 1u;
+  const uint64_t magic = div_t_magic(T);
   for (int64_t c0 = e0; c0 < e1; c0 += 32) {
     const int64_t e = c0 + lane;
     int a = -1;
     if (e < e1) {
-      const int64_t s = e / T;
+      const int64_t s = div_t(e, magic);
       const int t = (int)(e - s * T);
       if (t < nnz[s]) {
         const int v = idx[e];
@@ -178,6 +190,7 @@ prepare_kernel(const float* __restrict__ X, int n, int T, int Kp, const int32_t*
   // entries per warp batch: 2 keeps the kernel at <= 64 registers, two 512-thread CTAs per SM
   // (measured faster than 4 or 6 entries with one CTA per SM)
   constexpr int EB = NPL <= 16 ? 2 : 1;
+  const uint64_t magic = div_t_magic(T);
   // the list entries of the warp's next batch are loaded one batch ahead, so each batch costs
   // one round of loads (signals and code rows) instead of two
   int32_t ecur[EB];
@@ -193,7 +206,7 @@ prepare_kernel(const float* __restrict__ X, int n, int T, int Kp, const int32_t*
 #pragma unroll
     for (int b = 0; b < EB; ++b) {
       const int64_t e = b < ne ? ecur[b] : 0;
-      sg[b] = e / T;
+      sg[b] = div_t(e, magic);
       ts[b] = (int)(e - sg[b] * T);
     }
 #pragma unroll
@@ -607,9 +620,7 @@ struct Sweep {
     const int64_t per = (cnt + nctas - 1) / nctas;
     const int64_t qa = q0 + min(cnt, (int64_t)c * per), qb = q0 + min(cnt, (int64_t)(c + 1) * per);
     const int32_t* st = stage + buf * kStageCap;
-    // e / T as a multiply and shift: exact for e < 2^31, T <= 64 (the error e T / 2^40 < 2^-9
-    // stays below the 1/T gap to the next integer)
-    const uint64_t magic = ((1ull << 40) + (uint64_t)T - 1) / (uint64_t)T;
+    const uint64_t magic = div_t_magic(T);
     int my_use = 0;
     for (;;) {
       int bidx = 0;
@@ -623,7 +634,7 @@ struct Sweep {
       for (int b = 0; b < EB; ++b) {
         const int64_t q = qs + b;
         e[b] = b < ne ? (q - qa < kStageCap ? (int64_t)st[q - qa] : (int64_t)A.list[q]) : 0;
-        s[b] = (int64_t)(((uint64_t)e[b] * magic) >> 40);
+        s[b] = div_t(e[b], magic);
       }
       // the signal, its whole code row and its support size, all in one round of loads
       float xv[EB][NPL];
