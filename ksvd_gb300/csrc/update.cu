@@ -17,6 +17,8 @@
 //      with a grid barrier between phases; an atom no signal uses takes the special case
 //      (specialCase + SCase_*, DictionaryUpdate.cu:238-302, ReductionKernels.cu:436-539).
 //      Barrier waits are bounded: on timeout the kernel records kDevErrTimeout and returns.
+#include <type_traits>
+
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -29,14 +31,21 @@ constexpr int kSweepThreads = 512;
 constexpr int kStageCap = 2048;   // list entries of the next atom staged per CTA (x2 buffers)
 constexpr unsigned kBarrierSpinLimit = 1u << 24;   // x >= 64 ns sleeps: > 1 s before giving up
 
-// e / T for list entries e = signal * T + slot as a multiply and shift (magic = ceil(2^40 / T)):
-// exact for 0 <= e < 2^31 and 1 <= T <= 64, the error e T / 2^40 < 2^-9 staying below the 1/T
-// gap to the next integer.  The callers keep N * T < 2^31.
-__host__ __device__ inline uint64_t div_t_magic(int T) {
-  return ((1ull << 40) + (uint64_t)T - 1) / (uint64_t)T;
+// e / T for list entries e = signal * T + slot as a 32-bit multiply-high and a shift.  With
+// l = ceil(log2 T) and m = ceil(2^(31+l) / T) (< 2^32), m T - 2^(31+l) <= T - 1 < 2^l, so
+// floor(e / T) = floor(e m / 2^(31+l)) for every 0 <= e < 2^31 (Granlund & Montgomery, "Division
+// by invariant integers using multiplication", PLDI 1994, Thm 4.2 with 31-bit dividends);
+// mulhi(2 e, m) = floor(e m / 2^31) leaves a shift by l.  The callers keep N * T < 2^31.
+struct DivT {
+  uint32_t m, l;
+};
+__host__ __device__ inline DivT div_t_magic(int T) {
+  uint32_t l = 0;
+  while ((1ll << l) < (long long)T) ++l;
+  return {(uint32_t)((((uint64_t)1 << (31 + l)) + (uint64_t)T - 1) / (uint64_t)T), l};
 }
-__device__ __forceinline__ int64_t div_t(int64_t e, uint64_t magic) {
-  return (int64_t)(((uint64_t)e * magic) >> 40);
+__device__ __forceinline__ int div_t(int e, DivT d) {
+  return (int)(__umulhi((uint32_t)e << 1, d.m) >> d.l);
 }
 
 // ---- 1. atom lists --------------------------------------------------------------------------
@@ -52,10 +61,11 @@ __global__ void list_count_kernel(const int32_t* __restrict__ idx, const int32_t
   const int64_t s1 = min(N, s0 + kSigPerBlock);
   const int64_t e0 = s0 * T, e1 = s1 * T;
   bool bad = false;
-  const uint64_t magic = div_t_magic(T);
-  for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-    const int64_t s = div_t(e, magic);
-    const int t = (int)(e - s * T);
+  const DivT dt = div_t_magic(T);
+  for (int64_t e64 = e0 + threadIdx.x; e64 < e1; e64 += blockDim.x) {
+    const int e = (int)e64;                 // N * T < 2^31
+    const int s = div_t(e, dt);
+    const int t = e - s * T;
     if (t < nnz[s]) {
       const int a = idx[e];
       if (a >= 0 && a < K) atomicAdd(&hist[a], 1);
@@ -135,13 +145,13 @@ __global__ void list_fill_kernel(const int32_t* __restrict__ idx, const int32_t*
   const int64_t s1 = min(N, s0 + kSigPerBlock);
   const int64_t e0 = s0 * T, e1 = s1 * T;
   const unsigned lt_mask = (1u << lane) - 1u;
-  const uint64_t magic = div_t_magic(T);
+  const DivT dt = div_t_magic(T);
   for (int64_t c0 = e0; c0 < e1; c0 += 32) {
-    const int64_t e = c0 + lane;
+    const int e = (int)(c0 + lane);        // N * T < 2^31 (read only when c0 + lane < e1)
     int a = -1;
-    if (e < e1) {
-      const int64_t s = div_t(e, magic);
-      const int t = (int)(e - s * T);
+    if (c0 + lane < e1) {
+      const int s = div_t(e, dt);
+      const int t = e - s * T;
       if (t < nnz[s]) {
         const int v = idx[e];
         if (v >= 0 && v < K) a = v;
@@ -166,7 +176,8 @@ __global__ void list_fill_kernel(const int32_t* __restrict__ idx, const int32_t*
 // entries in flight, with its share of Y_j in registers (NPL rows per lane) and its share of
 // C(:,j) in a private shared-memory vector; the warp partials are summed in warp order at the
 // end, so the result is deterministic.
-template <int NPL>
+// CW: code-row words per lane (1 for T <= 32, else 2); FULLN: n == 32 NPL (no row test).
+template <int NPL, int CW, bool FULLN>
 __global__ void __launch_bounds__(kPrepThreads)
 prepare_kernel(const float* __restrict__ X, int n, int T, int Kp, const int32_t* __restrict__ idx,
                const float* __restrict__ coef, const int32_t* __restrict__ nnz,
@@ -190,7 +201,7 @@ prepare_kernel(const float* __restrict__ X, int n, int T, int Kp, const int32_t*
   // entries per warp batch: 2 keeps the kernel at <= 64 registers, two 512-thread CTAs per SM
   // (measured faster than 4 or 6 entries with one CTA per SM)
   constexpr int EB = NPL <= 16 ? 2 : 1;
-  const uint64_t magic = div_t_magic(T);
+  const DivT dt = div_t_magic(T);
   // the list entries of the warp's next batch are loaded one batch ahead, so each batch costs
   // one round of loads (signals and code rows) instead of two
   int32_t ecur[EB];
@@ -200,14 +211,15 @@ prepare_kernel(const float* __restrict__ X, int n, int T, int Kp, const int32_t*
     ecur[b] = q < q1 ? list[q] : 0;
   }
   for (int64_t qs = q0 + (int64_t)w * EB; qs < q1; qs += (int64_t)NW * EB) {
-    const int ne = (int)min((int64_t)EB, q1 - qs);
-    int64_t sg[EB];
-    int ts[EB];
+    const int ne = (int)min((int64_t)EB, q1 - qs);   // >= 1
+    int sg[EB], ts[EB];
+    bool live[EB];
 #pragma unroll
     for (int b = 0; b < EB; ++b) {
-      const int64_t e = b < ne ? ecur[b] : 0;
-      sg[b] = div_t(e, magic);
-      ts[b] = (int)(e - sg[b] * T);
+      live[b] = b == 0 || b < ne;
+      const int e = live[b] ? ecur[b] : 0;
+      sg[b] = div_t(e, dt);                  // entries e = signal * T + slot < 2^31
+      ts[b] = e - sg[b] * T;
     }
 #pragma unroll
     for (int b = 0; b < EB; ++b) {
@@ -217,37 +229,38 @@ prepare_kernel(const float* __restrict__ X, int n, int T, int Kp, const int32_t*
     // the signals, their whole code rows and support sizes: one round of independent loads
     float xv[EB][NPL];
 #pragma unroll
-    for (int b = 0; b < EB; ++b)
+    for (int b = 0; b < EB; ++b) {
+      const float* xp = X + (int64_t)sg[b] * n + lane;
 #pragma unroll
-      for (int i = 0; i < NPL; ++i) {
-        const int r = lane + 32 * i;
-        xv[b][i] = (b < ne && r < n) ? __ldg(X + sg[b] * n + r) : 0.f;
-      }
-    float cf[EB][2];
-    int ix[EB][2], nz[EB];
+      for (int i = 0; i < NPL; ++i)
+        xv[b][i] = (live[b] && (FULLN || lane + 32 * i < n)) ? __ldg(xp + 32 * i) : 0.f;
+    }
+    float cf[EB][CW];
+    int ix[EB][CW], nz[EB];
 #pragma unroll
     for (int b = 0; b < EB; ++b) {
-      nz[b] = b < ne ? nnz[sg[b]] : 0;
+      nz[b] = live[b] ? nnz[sg[b]] : 0;
+      const int cb = sg[b] * T;
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
+      for (int u = 0; u < CW; ++u) {
         const int t = lane + 32 * u;
-        const bool in = b < ne && t < T;
-        ix[b][u] = in ? idx[sg[b] * T + t] : -1;
-        cf[b][u] = in ? coef[sg[b] * T + t] : 0.f;
+        const bool in = live[b] && t < T;
+        ix[b][u] = in ? idx[cb + t] : -1;
+        cf[b][u] = in ? coef[cb + t] : 0.f;
       }
     }
 #pragma unroll
     for (int b = 0; b < EB; ++b) {
       // gamma_j(s) is slot ts of the code row
-      const float g = __shfl_sync(KSVD_FULL_MASK, (ts[b] >> 5) == 0 ? cf[b][0] : cf[b][1],
-                                  ts[b] & 31);
-      if (b >= ne) continue;
+      const float cs = (CW == 1 || (ts[b] >> 5) == 0) ? cf[b][0] : cf[b][CW - 1];
+      const float g = __shfl_sync(KSVD_FULL_MASK, cs, ts[b] & 31);
+      if (!live[b]) continue;
 #pragma unroll
       for (int i = 0; i < NPL; ++i) acc[i] = fmaf(g, xv[b][i], acc[i]);
       g2 = fmaf(g, g, g2);
       const int lim = min(nz[b], T);
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
+      for (int u = 0; u < CW; ++u) {
         const int t = lane + 32 * u;
         const int i = ix[b][u];
         if (t < lim && i >= 0 && i < Kp) cw[i] = fmaf(g, cf[b][u], cw[i]);   // distinct per signal
@@ -599,11 +612,12 @@ struct Sweep {
     const int64_t per = (cnt + nctas - 1) / nctas;
     const int64_t qa = q0 + min(cnt, (int64_t)c * per), qb = q0 + min(cnt, (int64_t)(c + 1) * per);
     int32_t* st = stage + buf * kStageCap;
+    const DivT dt = div_t_magic(A.T);
     for (int64_t q = qa + gt; q < qb; q += gsize) {
       const int32_t e = A.list[q];
       if (q - qa < kStageCap) st[q - qa] = e;
-      const int64_t s = e / A.T;
-      prefetch_l2_lines(A.X + s * A.n, (uint32_t)A.n * 4);
+      const int s = div_t(e, dt);
+      prefetch_l2_lines(A.X + (int64_t)s * A.n, (uint32_t)A.n * 4);
       prefetch_l2_lines(A.coef + s * A.T, (uint32_t)A.T * 4);
       prefetch_l2_lines(A.idx + s * A.T, (uint32_t)A.T * 4);
     }
@@ -620,7 +634,7 @@ struct Sweep {
     const int64_t per = (cnt + nctas - 1) / nctas;
     const int64_t qa = q0 + min(cnt, (int64_t)c * per), qb = q0 + min(cnt, (int64_t)(c + 1) * per);
     const int32_t* st = stage + buf * kStageCap;
-    const uint64_t magic = div_t_magic(T);
+    const DivT dt = div_t_magic(T);
     int my_use = 0;
     for (;;) {
       int bidx = 0;
@@ -629,33 +643,34 @@ struct Sweep {
       const int64_t qs = qa + (int64_t)bidx * EB;
       if (qs >= qb) break;
       const int ne = (int)min((int64_t)EB, qb - qs);
-      int64_t e[EB], s[EB];
+      int e[EB], s[EB];                      // entries e = signal * T + slot < 2^31
 #pragma unroll
       for (int b = 0; b < EB; ++b) {
         const int64_t q = qs + b;
-        e[b] = b < ne ? (q - qa < kStageCap ? (int64_t)st[q - qa] : (int64_t)A.list[q]) : 0;
-        s[b] = div_t(e[b], magic);
+        e[b] = b < ne ? (q - qa < kStageCap ? st[q - qa] : A.list[q]) : 0;
+        s[b] = div_t(e[b], dt);
       }
       // the signal, its whole code row and its support size, all in one round of loads
       float xv[EB][NPL];
 #pragma unroll
-      for (int b = 0; b < EB; ++b)
+      for (int b = 0; b < EB; ++b) {
+        const float* xp = A.X + (int64_t)s[b] * n + lane;
 #pragma unroll
-        for (int i = 0; i < NPL; ++i) {
-          const int r = lane + 32 * i;
-          xv[b][i] = (b < ne && r < n) ? __ldcg(A.X + s[b] * n + r) : 0.f;
-        }
+        for (int i = 0; i < NPL; ++i)
+          xv[b][i] = (b < ne && lane + 32 * i < n) ? __ldcg(xp + 32 * i) : 0.f;
+      }
       float cf[EB][2];
       int ix[EB][2], nz[EB];
 #pragma unroll
       for (int b = 0; b < EB; ++b) {
         nz[b] = b < ne ? A.nnz[s[b]] : 0;
+        const int cb = s[b] * T;
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
           const int t = lane + 32 * u;
           const bool in = b < ne && t < T;
-          ix[b][u] = in ? A.idx[s[b] * T + t] : -1;
-          cf[b][u] = in ? __ldcg(A.coef + s[b] * T + t) : 0.f;
+          ix[b][u] = in ? A.idx[cb + t] : -1;
+          cf[b][u] = in ? __ldcg(A.coef + cb + t) : 0.f;
         }
       }
 #pragma unroll
@@ -691,7 +706,7 @@ struct Sweep {
 #pragma unroll
       for (int b = 0; b < EB; ++b) {
         // gamma_j(s) is slot e % T of the code row already in registers
-        const int ts = (int)(e[b] - s[b] * T);
+        const int ts = e[b] - s[b] * T;
         gold[b] = __shfl_sync(KSVD_FULL_MASK, (ts >> 5) == 0 ? cf[b][0] : cf[b][1], ts & 31);
       }
       float gmine = 0.f;
@@ -932,11 +947,18 @@ cudaError_t launch_update_prepare(const UpdateArgs& a, cudaStream_t st) {
                                           a.start, a.Y, a.gn2, a.C);
     return cudaGetLastError();
   };
-  if (npl <= 2) e = launch(prepare_kernel<2>);
-  else if (npl <= 4) e = launch(prepare_kernel<4>);
-  else if (npl <= 8) e = launch(prepare_kernel<8>);
-  else if (npl <= 16) e = launch(prepare_kernel<16>);
-  else e = launch(prepare_kernel<32>);
+  const bool cw1 = a.T <= 32;
+  auto launch_npl = [&](auto npl_c) -> cudaError_t {
+    constexpr int P = decltype(npl_c)::value;
+    const bool full = a.n == 32 * P;
+    if (cw1) return full ? launch(prepare_kernel<P, 1, true>) : launch(prepare_kernel<P, 1, false>);
+    return full ? launch(prepare_kernel<P, 2, true>) : launch(prepare_kernel<P, 2, false>);
+  };
+  if (npl <= 2) e = launch_npl(std::integral_constant<int, 2>());
+  else if (npl <= 4) e = launch_npl(std::integral_constant<int, 4>());
+  else if (npl <= 8) e = launch_npl(std::integral_constant<int, 8>());
+  else if (npl <= 16) e = launch_npl(std::integral_constant<int, 16>());
+  else e = launch_npl(std::integral_constant<int, 32>());
   if (e != cudaSuccess) return e;
   // P = D'Y (P(i, j) = d_i . Y_j at P[j*Kp + i])
   return launch_gemm_tn_f32(a.D, a.n, a.Y, a.n, a.P, a.Kp, a.K, a.Kp, a.K, a.Kp, a.n, st);
