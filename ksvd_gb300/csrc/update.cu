@@ -172,6 +172,32 @@ __global__ void list_fill_kernel(const int32_t* __restrict__ idx, const int32_t*
 
 // ---- 2. per-atom precompute -------------------------------------------------------------------
 
+// Sums the NW warps' partials of C(:,j), Y(:,j) and ||gamma_j||^2 in warp order (deterministic).
+template <int NW>
+__device__ __forceinline__ void prepare_sum_warps(const float* Cw, const float* Yw,
+                                                  const float* g2w, int n, int Kp, int j,
+                                                  float* __restrict__ Y, float* __restrict__ gn2,
+                                                  float* __restrict__ C) {
+  for (int i = threadIdx.x; i < Kp; i += blockDim.x) {
+    float a = 0.f;
+#pragma unroll
+    for (int ww = 0; ww < NW; ++ww) a += Cw[(size_t)ww * Kp + i];
+    C[(int64_t)j * Kp + i] = a;
+  }
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    float a = 0.f;
+#pragma unroll
+    for (int ww = 0; ww < NW; ++ww) a += Yw[(size_t)ww * n + r];
+    Y[(int64_t)j * n + r] = a;
+  }
+  if (threadIdx.x == 0) {
+    float a = 0.f;
+#pragma unroll
+    for (int ww = 0; ww < NW; ++ww) a += g2w[ww];
+    gn2[j] = a;
+  }
+}
+
 // CTA j: gn2[j], Y(:,j), C(:,j) from the atom's list.  Each warp walks every 8th entry, two
 // entries in flight, with its share of Y_j in registers (NPL rows per lane) and its share of
 // C(:,j) in a private shared-memory vector; the warp partials are summed in warp order at the
@@ -275,24 +301,100 @@ prepare_kernel(const float* __restrict__ X, int n, int T, int Kp, const int32_t*
   }
   if (lane == 0) g2w[w] = g2;
   __syncthreads();
-  for (int i = threadIdx.x; i < Kp; i += blockDim.x) {
-    float a = 0.f;
+  prepare_sum_warps<NW>(Cw, Yw, g2w, n, Kp, j, Y, gn2, C);
+}
+
+// Half-warp variant for T <= 16, n % 4 == 0, n <= 64 NQ and a 16-byte aligned X: each half-warp
+// takes one list entry (a warp two consecutive entries), a lane gathers four consecutive rows per
+// 16-byte load and holds slot (lane & 15) of the code row, so the per-entry bookkeeping (the
+// division by T, the code-row loads, the shuffle for gamma_j(s)) is issued once for two entries.
+// The halves' C(:,j) updates go one after the other (two signals of atom j's list can share
+// other atoms); Y and ||gamma_j||^2 partials are combined at the end, in a fixed order.
+template <int NQ, bool FULLN>
+__global__ void __launch_bounds__(kPrepThreads)
+prepare_half_kernel(const float* __restrict__ X, int n, int T, int Kp,
+                    const int32_t* __restrict__ idx, const float* __restrict__ coef,
+                    const int32_t* __restrict__ nnz, const int32_t* __restrict__ list,
+                    const int64_t* __restrict__ start, float* __restrict__ Y,
+                    float* __restrict__ gn2, float* __restrict__ C) {
+  constexpr int NW = kPrepThreads / 32;
+  extern __shared__ float sm[];
+  float* Cw = sm;                        // NW x Kp
+  float* Yw = sm + (size_t)NW * Kp;      // NW x n
+  __shared__ float g2w[NW];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int hl = lane & 15, half = lane >> 4;
+  const int j = blockIdx.x;
+  for (int i = threadIdx.x; i < NW * Kp; i += blockDim.x) Cw[i] = 0.f;
+  __syncthreads();
+  const int64_t q0 = start[j], q1 = start[j + 1];
+  float* cw = Cw + (size_t)w * Kp;
+  float4 acc[NQ];
 #pragma unroll
-    for (int ww = 0; ww < NW; ++ww) a += Cw[(size_t)ww * Kp + i];
-    C[(int64_t)j * Kp + i] = a;
+  for (int k = 0; k < NQ; ++k) acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+  float g2 = 0.f;
+  const DivT dt = div_t_magic(T);
+  // this half's entry of the warp's next pair, loaded one pair ahead
+  int ecur = 0;
+  {
+    const int64_t q = q0 + 2 * w + half;
+    if (q < q1) ecur = list[q];
   }
-  for (int r = threadIdx.x; r < n; r += blockDim.x) {
-    float a = 0.f;
+  for (int64_t qs = q0 + 2 * w; qs < q1; qs += 2 * NW) {
+    const bool live = qs + half < q1;
+    const int e = live ? ecur : 0;
+    const int s = div_t(e, dt);            // entries e = signal * T + slot < 2^31
+    const int ts = e - s * T;
+    {
+      const int64_t qn = qs + 2 * NW + half;
+      ecur = qn < q1 ? list[qn] : 0;
+    }
+    // the signal (4 consecutive rows per load), the code row slot and the support size
+    const float4* xp = reinterpret_cast<const float4*>(X + (int64_t)s * n) + hl;
+    float4 xv[NQ];
 #pragma unroll
-    for (int ww = 0; ww < NW; ++ww) a += Yw[(size_t)ww * n + r];
-    Y[(int64_t)j * n + r] = a;
-  }
-  if (threadIdx.x == 0) {
-    float a = 0.f;
+    for (int k = 0; k < NQ; ++k)
+      xv[k] = (live && (FULLN || 4 * hl + 64 * k < n)) ? __ldg(xp + 16 * k)
+                                                       : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int nz = live ? nnz[s] : 0;
+    const bool in = live && hl < T;
+    const int ix = in ? idx[s * T + hl] : -1;
+    const float cf = in ? coef[s * T + hl] : 0.f;
+    // gamma_j(s) is slot ts (< T <= 16) of this half's code row; 0 for a dead half
+    const float g = __shfl_sync(KSVD_FULL_MASK, cf, (lane & 16) | ts);
 #pragma unroll
-    for (int ww = 0; ww < NW; ++ww) a += g2w[ww];
-    gn2[j] = a;
+    for (int k = 0; k < NQ; ++k) {
+      acc[k].x = fmaf(g, xv[k].x, acc[k].x);
+      acc[k].y = fmaf(g, xv[k].y, acc[k].y);
+      acc[k].z = fmaf(g, xv[k].z, acc[k].z);
+      acc[k].w = fmaf(g, xv[k].w, acc[k].w);
+    }
+    g2 = fmaf(g, g, g2);
+    const bool ok = hl < min(nz, T) && (unsigned)ix < (unsigned)Kp;
+    if (half == 0 && ok) cw[ix] = fmaf(g, cf, cw[ix]);   // distinct atoms within one signal
+    __syncwarp();
+    if (half == 1 && ok) cw[ix] = fmaf(g, cf, cw[ix]);
+    __syncwarp();
   }
+  // half 1's partials into half 0
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    acc[k].x += __shfl_down_sync(KSVD_FULL_MASK, acc[k].x, 16);
+    acc[k].y += __shfl_down_sync(KSVD_FULL_MASK, acc[k].y, 16);
+    acc[k].z += __shfl_down_sync(KSVD_FULL_MASK, acc[k].z, 16);
+    acc[k].w += __shfl_down_sync(KSVD_FULL_MASK, acc[k].w, 16);
+  }
+  g2 += __shfl_down_sync(KSVD_FULL_MASK, g2, 16);
+  if (half == 0) {
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+      const int r = 4 * hl + 64 * k;
+      if (FULLN || r < n) *reinterpret_cast<float4*>(Yw + (size_t)w * n + r) = acc[k];
+    }
+  }
+  if (lane == 0) g2w[w] = g2;
+  __syncthreads();
+  prepare_sum_warps<NW>(Cw, Yw, g2w, n, Kp, j, Y, gn2, C);
 }
 
 __global__ void init_state_kernel(int64_t N, int Kp, int32_t* __restrict__ unused,
@@ -452,7 +554,7 @@ struct Sweep {
   __device__ Sweep(const SweepArgs& a, float* sm, float* rf, int* ri, int* sf)
       : A(a), red_f(rf), red_i(ri), sflag(sf) {
     a_s = sm;
-    aD_s = a_s + A.n;
+    aD_s = a_s + round_up(A.n, 4);        // v_s is read as float4: 16-byte aligned for any n
     cpart = aD_s + A.Kp;
     v_s = cpart + A.Kp;
     stage = reinterpret_cast<int32_t*>(v_s + A.Kp);
@@ -954,7 +1056,18 @@ cudaError_t launch_update_prepare(const UpdateArgs& a, cudaStream_t st) {
     if (cw1) return full ? launch(prepare_kernel<P, 1, true>) : launch(prepare_kernel<P, 1, false>);
     return full ? launch(prepare_kernel<P, 2, true>) : launch(prepare_kernel<P, 2, false>);
   };
-  if (npl <= 2) e = launch_npl(std::integral_constant<int, 2>());
+  auto launch_nq = [&](auto nq_c) -> cudaError_t {
+    constexpr int Q = decltype(nq_c)::value;
+    return a.n == 64 * Q ? launch(prepare_half_kernel<Q, true>)
+                         : launch(prepare_half_kernel<Q, false>);
+  };
+  // the half-warp kernel when its layout fits (rows of X 16-byte aligned, one slot per lane)
+  const bool half = a.T <= 16 && a.n % 4 == 0 && a.n <= 256 &&
+                    (reinterpret_cast<uintptr_t>(a.X) & 15) == 0;
+  if (half && a.n <= 64) e = launch_nq(std::integral_constant<int, 1>());
+  else if (half && a.n <= 128) e = launch_nq(std::integral_constant<int, 2>());
+  else if (half) e = launch_nq(std::integral_constant<int, 4>());
+  else if (npl <= 2) e = launch_npl(std::integral_constant<int, 2>());
   else if (npl <= 4) e = launch_npl(std::integral_constant<int, 4>());
   else if (npl <= 8) e = launch_npl(std::integral_constant<int, 8>());
   else if (npl <= 16) e = launch_npl(std::integral_constant<int, 16>());
@@ -973,7 +1086,7 @@ cudaError_t launch_update_sweep(const UpdateArgs& a, cudaStream_t st) {
   s.avec = a.avec; s.aDbuf = a.aD; s.part = a.part; s.unused = a.unused; s.bitmap = a.bitmap;
   s.replaced = a.replaced; s.counter = a.counter; s.usecount = a.usecount; s.barrier = a.barrier;
   s.dev_err = a.dev_err;
-  const size_t smem = sizeof(float) * ((size_t)a.n + 3 * (size_t)a.Kp) +
+  const size_t smem = sizeof(float) * ((size_t)round_up(a.n, 4) + 3 * (size_t)a.Kp) +
                       sizeof(int32_t) * (2 * kStageCap + (size_t)a.Kp);
   const int npl = (a.n + 31) / 32;
   auto launch = [&](auto kern) -> cudaError_t {

@@ -145,10 +145,15 @@ def code_from_oracle(oracle_mod, X, D, T):
     return oracle_mod.omp(oracle_mod.gram(D64), oracle_mod.dtx(D64, X64), T)
 
 
+# the list preparation has a half-warp kernel (T <= 16, n % 4 == 0, n <= 256) and a full-warp one:
+# the first three and (200, ...) take the half-warp kernel, (50, ...) and (96, ..., 20) the other
 @pytest.mark.parametrize("n,K,N,T,seed,unused_atom", [
     (64, 256, 8000, 8, 20, False),
     (256, 1024, 20000, 16, 21, False),
     (40, 64, 3000, 4, 22, True),
+    (200, 512, 6000, 10, 23, False),
+    (50, 128, 4000, 6, 24, False),
+    (96, 256, 5000, 20, 25, False),
 ])
 def test_update_matches_oracle(oracle_mod, cuda, n, K, N, T, seed, unused_atom):
     import torch
