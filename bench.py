@@ -71,6 +71,17 @@ class ClockSampler:
                 stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        # nvidia-smi takes a moment to start: wait for its first row, so the samples cover the
+        # timed region that follows
+        t0 = time.time()
+        while time.time() - t0 < 5.0 and self.proc.poll() is None:
+            try:
+                if os.path.getsize(self.f.name) > 0:
+                    break
+            except OSError:
+                break
+            time.sleep(0.05)
 
     def stop(self):
         if not self.proc:
