@@ -94,6 +94,100 @@ error_kernel(ErrorArgs A) {
   }
 }
 
+// Half-warp variant for T <= 16, n % 4 == 0, n <= 64 NQ and 16-byte aligned X and D: each half
+// of a warp reconstructs one signal (four consecutive rows per 16-byte load, slot lane & 15 of the
+// code row per lane), so the per-column shuffles and address arithmetic are issued once for two
+// signals.  The halves walk ascending signals and are combined at the end (sum, then the larger
+// error with the lower signal on ties), so the results stay deterministic.
+template <int NQ, bool FULLN>
+__global__ void __launch_bounds__(kErrWarps * 32)
+error_half_kernel(ErrorArgs A) {
+  __shared__ double wsum[kErrWarps];
+  __shared__ float wval[kErrWarps];
+  __shared__ int64_t widx[kErrWarps];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int hl = lane & 15, hbase = lane & 16;
+  const int n = A.n, T = A.T;
+  const int64_t b = blockIdx.x;
+  const int64_t s0 = b * kBucket, s1 = min(A.N, s0 + kBucket);
+  double sum = 0.0;
+  float bv = -1.f;
+  int64_t bi = INT64_MAX;
+  bool bad = false;
+  for (int64_t sp = s0 + 2 * w; sp < s1; sp += 2 * kErrWarps) {
+    const int64_t s = sp + (lane >> 4);
+    const bool live = s < s1;
+    const float4* xp = reinterpret_cast<const float4*>(A.X + (live ? s : sp) * n) + hl;
+    float4 acc[NQ];
+#pragma unroll
+    for (int k = 0; k < NQ; ++k)
+      acc[k] = (live && (FULLN || 4 * hl + 64 * k < n)) ? __ldcs(xp + 16 * k)
+                                                        : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int nz = live ? min(A.nnz[s], T) : 0;
+    const bool in = hl < nz;
+    const int kraw = in ? A.idx[s * T + hl] : -1;
+    const bool ok = (unsigned)kraw < (unsigned)A.K;
+    bad |= in && !ok;
+    const int kk = (in && ok) ? kraw : -1;
+    const float gg = (in && ok) ? A.coef[s * T + hl] : 0.f;
+    const int nzw = max(nz, __shfl_xor_sync(KSVD_FULL_MASK, nz, 16));
+#pragma unroll 4
+    for (int t = 0; t < nzw; ++t) {
+      const int k = __shfl_sync(KSVD_FULL_MASK, kk, hbase | t);
+      const float g = __shfl_sync(KSVD_FULL_MASK, gg, hbase | t);
+      if (k < 0) continue;
+      const float4* dp = reinterpret_cast<const float4*>(A.D + (int64_t)k * n) + hl;
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        if (!FULLN && 4 * hl + 64 * q >= n) continue;
+        const float4 d = __ldg(dp + 16 * q);
+        acc[q].x = fmaf(-g, d.x, acc[q].x);
+        acc[q].y = fmaf(-g, d.y, acc[q].y);
+        acc[q].z = fmaf(-g, d.z, acc[q].z);
+        acc[q].w = fmaf(-g, d.w, acc[q].w);
+      }
+    }
+    float e = 0.f;
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+      e = fmaf(acc[k].x, acc[k].x, e);
+      e = fmaf(acc[k].y, acc[k].y, e);
+      e = fmaf(acc[k].z, acc[k].z, e);
+      e = fmaf(acc[k].w, acc[k].w, e);
+    }
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) e += __shfl_xor_sync(KSVD_FULL_MASK, e, o);
+    if (live) {
+      sum += (double)e;
+      const float em = A.bitmap ? e * (float)A.bitmap[s] : e;
+      if (hl == 0) A.err[s] = em;
+      if (em > bv) { bv = em; bi = s; }      // s ascends within the half: first maximum kept
+    }
+  }
+  // half 1 into half 0
+  sum += __shfl_down_sync(KSVD_FULL_MASK, sum, 16);
+  {
+    const float ov = __shfl_down_sync(KSVD_FULL_MASK, bv, 16);
+    const long long oi = __shfl_down_sync(KSVD_FULL_MASK, (long long)bi, 16);
+    if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+  }
+  if (__any_sync(KSVD_FULL_MASK, bad) && lane == 0 && A.dev_err) atomicOr(A.dev_err, kDevErrBounds);
+  if (lane == 0) { wsum[w] = sum; wval[w] = bv; widx[w] = bi; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    float v = -1.f;
+    int64_t vi = INT64_MAX;
+    for (int ww = 0; ww < kErrWarps; ++ww) {
+      t += wsum[ww];
+      if (wval[ww] > v || (wval[ww] == v && widx[ww] < vi)) { v = wval[ww]; vi = widx[ww]; }
+    }
+    A.part_sum[b] = t;
+    A.bucket_val[b] = v;
+    A.bucket_idx[b] = vi;
+  }
+}
+
 __global__ void rmse_kernel(const double* __restrict__ part, int64_t nb, double denom,
                             double* __restrict__ out, const int* __restrict__ iter_ctr) {
   __shared__ double red[32];
@@ -247,7 +341,16 @@ cudaError_t launch_error(const ErrorArgs& a, cudaStream_t st) {
   if (a.n > kMaxN) return cudaErrorInvalidValue;
   const int64_t nb = error_block_count(a.N);
   const int npl = (a.n + 31) / 32;
-  if (npl <= 2) error_kernel<2><<<(unsigned)nb, kErrWarps * 32, 0, st>>>(a);
+  auto al16 = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
+  const bool half = a.T <= 16 && a.n % 4 == 0 && a.n <= 256 && al16(a.X) && al16(a.D);
+  const dim3 grid((unsigned)nb), blk(kErrWarps * 32);
+  if (half && a.n == 64) error_half_kernel<1, true><<<grid, blk, 0, st>>>(a);
+  else if (half && a.n < 64) error_half_kernel<1, false><<<grid, blk, 0, st>>>(a);
+  else if (half && a.n == 128) error_half_kernel<2, true><<<grid, blk, 0, st>>>(a);
+  else if (half && a.n < 128) error_half_kernel<2, false><<<grid, blk, 0, st>>>(a);
+  else if (half && a.n == 256) error_half_kernel<4, true><<<grid, blk, 0, st>>>(a);
+  else if (half) error_half_kernel<4, false><<<grid, blk, 0, st>>>(a);
+  else if (npl <= 2) error_kernel<2><<<(unsigned)nb, kErrWarps * 32, 0, st>>>(a);
   else if (npl <= 4) error_kernel<4><<<(unsigned)nb, kErrWarps * 32, 0, st>>>(a);
   else if (npl <= 8) error_kernel<8><<<(unsigned)nb, kErrWarps * 32, 0, st>>>(a);
   else if (npl <= 16) error_kernel<16><<<(unsigned)nb, kErrWarps * 32, 0, st>>>(a);
