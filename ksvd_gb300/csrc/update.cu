@@ -534,7 +534,9 @@ struct SweepArgs {
   int* dev_err;
 };
 
-template <int NPL>
+// HW: coefficient batches by half-warps (T <= 16, n % 4 == 0, n <= 64 (NPL / 2), X 16-byte
+// aligned); FULLN: n == 32 NPL.
+template <int NPL, bool HW = false, bool FULLN = false>
 struct Sweep {
   static constexpr int NW = kSweepThreads / 32;
   static constexpr int HALF = kSweepThreads / 2;                  // threads per warp group
@@ -725,12 +727,125 @@ struct Sweep {
     }
   }
 
+  // update_coefs with half-warps: half h of a warp takes entries h, h + 2, ... of the batch,
+  // loads its signal four rows per 16-byte load and slot (lane & 15) of its code row, so a warp
+  // instruction serves two entries; the per-entry sums share one 16-lane shuffle tree.
+  __device__ void update_coefs_half(int j, int64_t q0, int64_t cnt, float anorm, int buf,
+                                    int* next, int* use_cnt) {
+    constexpr int NQ = NPL / 2;            // float4 rows per lane
+    constexpr int EH = EB / 2;             // entries per half
+    static_assert(EB == 2 * EH && EH >= 1 && EH <= 2, "half-warp batches hold 2 or 4 entries");
+    const int n = A.n, K = A.K, T = A.T;
+    const int hl = lane & 15, hb = lane & 16, half = lane >> 4;
+    const float aDj = aD_s[j];
+    const int64_t per = (cnt + nctas - 1) / nctas;
+    const int64_t qa = q0 + min(cnt, (int64_t)c * per), qb = q0 + min(cnt, (int64_t)(c + 1) * per);
+    const int32_t* st = stage + buf * kStageCap;
+    const DivT dt = div_t_magic(T);
+    // this lane's rows of a(j), fixed through the phase (rows >= n are never read)
+    float4 av[NQ];
+#pragma unroll
+    for (int k = 0; k < NQ; ++k)
+      av[k] = (FULLN || 4 * hl + 64 * k < n) ? reinterpret_cast<const float4*>(a_s)[hl + 16 * k]
+                                             : make_float4(0.f, 0.f, 0.f, 0.f);
+    int my_use = 0;
+    for (;;) {
+      int bidx = 0;
+      if (lane == 0) bidx = atomicAdd(next, 1);
+      bidx = __shfl_sync(KSVD_FULL_MASK, bidx, 0);
+      const int64_t qs = qa + (int64_t)bidx * EB;
+      if (qs >= qb) break;
+      const int ne = (int)min((int64_t)EB, qb - qs);
+      int e[EH], s[EH];                      // entries e = signal * T + slot < 2^31
+      bool live[EH];
+#pragma unroll
+      for (int m = 0; m < EH; ++m) {
+        const int b = 2 * m + half;
+        const int64_t q = qs + b;
+        live[m] = b < ne;
+        e[m] = live[m] ? (q - qa < kStageCap ? st[q - qa] : A.list[q]) : 0;
+        s[m] = div_t(e[m], dt);
+      }
+      // the signal, its code row slot and its support size, all in one round of loads
+      float4 xv[EH][NQ];
+#pragma unroll
+      for (int m = 0; m < EH; ++m) {
+        const float4* xp = reinterpret_cast<const float4*>(A.X + (int64_t)s[m] * n) + hl;
+#pragma unroll
+        for (int k = 0; k < NQ; ++k)
+          xv[m][k] = (live[m] && (FULLN || 4 * hl + 64 * k < n)) ? __ldcg(xp + 16 * k)
+                                                                : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      float cf[EH];
+      int ix[EH], nz[EH];
+#pragma unroll
+      for (int m = 0; m < EH; ++m) {
+        nz[m] = live[m] ? A.nnz[s[m]] : 0;
+        const bool in = live[m] && hl < T;
+        ix[m] = in ? A.idx[s[m] * T + hl] : -1;
+        cf[m] = in ? __ldcg(A.coef + s[m] * T + hl) : 0.f;
+      }
+      float dpart[EH], gold[EH];
+#pragma unroll
+      for (int m = 0; m < EH; ++m) {
+        const bool ok = hl < min(nz[m], T) && (unsigned)ix[m] < (unsigned)K;
+        ix[m] = ok ? ix[m] : -1;
+        cf[m] = ok ? cf[m] : 0.f;
+        // gamma_j(s) is slot e % T (< T <= 16) of the code row
+        gold[m] = __shfl_sync(KSVD_FULL_MASK, cf[m], hb | (e[m] - s[m] * T));
+        // this lane's part of a.x_s - Gamma(:,s).(a'D)
+        float acc = 0.f;
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) {
+          acc = fmaf(av[k].x, xv[m][k].x, acc);
+          acc = fmaf(av[k].y, xv[m][k].y, acc);
+          acc = fmaf(av[k].z, xv[m][k].z, acc);
+          acc = fmaf(av[k].w, xv[m][k].w, acc);
+        }
+        if (ix[m] >= 0) acc = fmaf(-cf[m], aD_s[ix[m]], acc);
+        dpart[m] = acc;
+      }
+      // sums over each half: with EH = 2 the first level splits the entries (lanes with bit 8
+      // keep entry 1), so lane holds the sum of entry (lane >> 3) & (EH - 1) of its half
+      float dsum;
+      if constexpr (EH == 2) {
+        const bool u8 = lane & 8;
+        dsum = (u8 ? dpart[1] : dpart[0]) +
+               __shfl_xor_sync(KSVD_FULL_MASK, u8 ? dpart[0] : dpart[1], 8);
+      } else {
+        dsum = dpart[0] + __shfl_xor_sync(KSVD_FULL_MASK, dpart[0], 8);
+      }
+      dsum += __shfl_xor_sync(KSVD_FULL_MASK, dsum, 4);
+      dsum += __shfl_xor_sync(KSVD_FULL_MASK, dsum, 2);
+      dsum += __shfl_xor_sync(KSVD_FULL_MASK, dsum, 1);
+      const int mm = (lane >> 3) & (EH - 1);
+      const float go = (EH == 2 && mm == 1) ? gold[EH - 1] : gold[0];
+      const float gmine = (dsum + aDj * go) / anorm;
+#pragma unroll
+      for (int m = 0; m < EH; ++m) {
+        const float g = __shfl_sync(KSVD_FULL_MASK, gmine, hb | (m << 3));
+        if (!live[m]) continue;
+        if (ix[m] >= 0 && ix[m] != j) atomicAdd(cpart + ix[m], g * cf[m]);
+        if (hl == 0) {
+          A.coef[e[m]] = g;
+          if (g * g > 1e-7f) ++my_use;
+        }
+      }
+    }
+    my_use += __shfl_down_sync(KSVD_FULL_MASK, my_use, 16);
+    if (lane == 0 && my_use) atomicAdd(use_cnt, my_use);
+  }
+
   // New coefficients of atom j for this CTA's share of its signals, by warps [0, gnw).  Adds
   // into cpart (C row j) and *use_cnt; the caller synchronises and flushes.
   // Warps pull batches of EB entries from a shared counter (*next, zeroed before the phase), so
   // the warps that finish their other work of the phase join in.
   __device__ void update_coefs(int j, int64_t q0, int64_t cnt, float anorm, int buf, int* next,
                                int* use_cnt) {
+    if constexpr (HW) {
+      update_coefs_half(j, q0, cnt, anorm, buf, next, use_cnt);
+      return;
+    }
     const int n = A.n, K = A.K, T = A.T;
     const float aDj = aD_s[j];
     const int64_t per = (cnt + nctas - 1) / nctas;
@@ -917,7 +1032,7 @@ struct Sweep {
   }
 };
 
-template <int NPL>
+template <int NPL, bool HW, bool FULLN>
 __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
   extern __shared__ float sm[];
   __shared__ float red_f[64];
@@ -925,9 +1040,9 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
   __shared__ int sflag;
   __shared__ int use_cnt;
   __shared__ int next_batch;
-  Sweep<NPL> S(A, sm, red_f, red_i, &sflag);
+  Sweep<NPL, HW, FULLN> S(A, sm, red_f, red_i, &sflag);
   const int K = A.K, n = A.n, tid = threadIdx.x;
-  constexpr int HALF = Sweep<NPL>::HALF;
+  constexpr int HALF = Sweep<NPL, HW, FULLN>::HALF;
   const int32_t* perm = A.perm + (A.iter_ctr ? (int64_t)(*A.iter_ctr) * K : 0);
   // fewer than ~50 list entries per atom and CTA on average (measured: 26 faster, 103 slower)
   const bool light = A.N * A.T < 50LL * K * gridDim.x;
@@ -1103,11 +1218,20 @@ cudaError_t launch_update_sweep(const UpdateArgs& a, cudaStream_t st) {
     return cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(kSweepThreads), args,
                                        smem, st);
   };
-  if (npl <= 2) return launch(sweep_kernel<2>);
-  if (npl <= 4) return launch(sweep_kernel<4>);
-  if (npl <= 8) return launch(sweep_kernel<8>);
-  if (npl <= 16) return launch(sweep_kernel<16>);
-  return launch(sweep_kernel<32>);
+  // half-warp coefficient batches when their layout fits (as in the half-warp preparation)
+  const bool hw = a.T <= 16 && a.n % 4 == 0 && a.n <= 256 &&
+                  (reinterpret_cast<uintptr_t>(a.X) & 15) == 0;
+  if (hw && a.n <= 64) return a.n == 64 ? launch(sweep_kernel<2, true, true>)
+                                        : launch(sweep_kernel<2, true, false>);
+  if (hw && a.n <= 128) return a.n == 128 ? launch(sweep_kernel<4, true, true>)
+                                          : launch(sweep_kernel<4, true, false>);
+  if (hw) return a.n == 256 ? launch(sweep_kernel<8, true, true>)
+                            : launch(sweep_kernel<8, true, false>);
+  if (npl <= 2) return launch(sweep_kernel<2, false, false>);
+  if (npl <= 4) return launch(sweep_kernel<4, false, false>);
+  if (npl <= 8) return launch(sweep_kernel<8, false, false>);
+  if (npl <= 16) return launch(sweep_kernel<16, false, false>);
+  return launch(sweep_kernel<32, false, false>);
 }
 
 int update_sweep_ctas() { return sweep_grid_size(); }
