@@ -16,6 +16,7 @@ same workload, scaled to the full workload.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import math
 import os
@@ -752,6 +753,10 @@ def main():
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
+        # no Python garbage collection inside the timed calls (as timeit does): a collection of
+        # the benchmark's own objects is not the library's time
+        gc.collect()
+        gc.disable()
         t0 = time.perf_counter()
         # each call copies X and D in, runs one iteration, copies D and the code out and
         # synchronises; the per-call times are kept (the host's copies vary from call to call)
@@ -762,7 +767,9 @@ def main():
             h.iterate_host(Dn, Xn, 1, out=(oi, oc, on))
             per.append((time.perf_counter() - t1) * 1e3)
         torch.cuda.synchronize()
-        te = max_over_ranks(time.perf_counter() - t0, dist, dev)
+        te = time.perf_counter() - t0
+        gc.enable()
+        te = max_over_ranks(te, dist, dev)
         e2e = {"value": aggregate_rate(1, e2e_steps, te * 1e3, ws), "unit": "iter/s",
                "h2d_bytes_per_step": int(X.numel() * 4 + D.numel() * 4),
                "d2h_bytes_per_step": int(D.numel() * 4 + N * cfg.T * 8 + N * 4 + 8),
