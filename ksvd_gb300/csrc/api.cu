@@ -102,7 +102,7 @@ enum BufId {
   B_DPAD, B_G, B_A0, B_XN2, B_LIST, B_START, B_BHIST, B_Y, B_GN2, B_C, B_AVEC, B_AD, B_PART,
   B_UNUSED, B_BITMAP, B_REPLACED, B_COUNTER, B_USE, B_BARRIER, B_ERR, B_PSUM, B_BVAL, B_BIDX,
   B_RMSE, B_M, B_MI, B_CLEARED, B_DEVERR, B_PERM, B_GPAD_IN, B_HX, B_HD, B_HIDX, B_HCOEF, B_HNNZ,
-  B_XHI, B_XLO, B_DHI, B_DLO, B_P, B_BG, B_BA0, B_BDESC, B_BJOB, B_BQUEUE, B_ITER, B_RPART, B_RMEAN, B_TUNE_D, B_TUNE_C, B_GH, B_MU, B_OMPQ, B_COUNT
+  B_XHI, B_XLO, B_DHI, B_DLO, B_P, B_BG, B_BA0, B_BDESC, B_BJOB, B_BQUEUE, B_ITER, B_RPART, B_RMEAN, B_TUNE_D, B_TUNE_C, B_GH, B_MU, B_OMPQ, B_PREP_PART, B_COUNT
 };
 
 ksvd_status fail(ksvd_handle* h, ksvd_status s, const char* fmt, const char* detail = nullptr) {
@@ -388,6 +388,11 @@ ksvd_status update_ws(ksvd_handle* h, int64_t N, UpdateArgs& u) {
   KSVD_TRY(ensure(h, B_USE, (size_t)Kp, &u.usecount));
   KSVD_TRY(ensure(h, B_BARRIER, 2, &u.barrier));
   KSVD_TRY(ensure(h, B_DEVERR, 1, &u.dev_err));
+  u.prep_win = prepare_window_signals(N, n, h->p.T);
+  if (u.prep_win > 0) {
+    const int64_t nwin = (N + u.prep_win - 1) / u.prep_win;
+    KSVD_TRY(ensure(h, B_PREP_PART, (size_t)nwin * Kp * (n + Kp + 1), &u.prep_part));
+  }
   u.n = n; u.K = h->p.K; u.Kp = Kp; u.T = h->p.T; u.N = N;
   u.max_signals = h->p.max_replace_signals;
   u.sweep_ctas = h->sweep_ctas;

@@ -97,8 +97,15 @@ struct UpdateArgs {
   int32_t* usecount;     // Kp
   unsigned int* barrier; // 2 words
   int* dev_err;
+  // nullable: windowed list preparation (prep_win signals per window, partials in prep_part:
+  // ceil(N / prep_win) x Kp x (n + Kp + 1) floats); see prepare_window_signals
+  float* prep_part;
+  int64_t prep_win;
 };
 cudaError_t launch_update_prepare(const UpdateArgs& a, cudaStream_t st);
+// Signals per window of the windowed list preparation for this shape, or 0 when X fits L2 well
+// enough (or the half-warp layout does not apply) and one pass over each atom's list is used.
+int64_t prepare_window_signals(int64_t N, int n, int T);
 cudaError_t launch_update_sweep(const UpdateArgs& a, cudaStream_t st);
 int64_t update_block_count(int64_t N);
 int update_sweep_ctas();

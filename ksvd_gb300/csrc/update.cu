@@ -27,6 +27,7 @@ namespace {
 
 constexpr int kSigPerBlock = 256;      // signals per list-building block
 constexpr int kPrepThreads = 512;
+constexpr int kPrepWinThreads = 256;   // windowed preparation: four CTAs per SM
 constexpr int kSweepThreads = 512;
 constexpr int kStageCap = 2048;   // list entries of the next atom staged per CTA (x2 buffers)
 constexpr unsigned kBarrierSpinLimit = 1u << 24;   // x >= 64 ns sleeps: > 1 s before giving up
@@ -304,30 +305,20 @@ prepare_kernel(const float* __restrict__ X, int n, int T, int Kp, const int32_t*
   prepare_sum_warps<NW>(Cw, Yw, g2w, n, Kp, j, Y, gn2, C);
 }
 
-// Half-warp variant for T <= 16, n % 4 == 0, n <= 64 NQ and a 16-byte aligned X: each half-warp
-// takes one list entry (a warp two consecutive entries), a lane gathers four consecutive rows per
-// 16-byte load and holds slot (lane & 15) of the code row, so the per-entry bookkeeping (the
-// division by T, the code-row loads, the shuffle for gamma_j(s)) is issued once for two entries.
-// The halves' C(:,j) updates go one after the other (two signals of atom j's list can share
-// other atoms); Y and ||gamma_j||^2 partials are combined at the end, in a fixed order.
-template <int NQ, bool FULLN>
-__global__ void __launch_bounds__(kPrepThreads)
-prepare_half_kernel(const float* __restrict__ X, int n, int T, int Kp,
-                    const int32_t* __restrict__ idx, const float* __restrict__ coef,
-                    const int32_t* __restrict__ nnz, const int32_t* __restrict__ list,
-                    const int64_t* __restrict__ start, float* __restrict__ Y,
-                    float* __restrict__ gn2, float* __restrict__ C) {
-  constexpr int NW = kPrepThreads / 32;
-  extern __shared__ float sm[];
-  float* Cw = sm;                        // NW x Kp
-  float* Yw = sm + (size_t)NW * Kp;      // NW x n
-  __shared__ float g2w[NW];
+// Half-warp preparation of list entries [q0, q1) of atom j, for T <= 16, n % 4 == 0, n <= 64 NQ
+// and a 16-byte aligned X: each half-warp takes one list entry (a warp two consecutive entries),
+// a lane gathers four consecutive rows per 16-byte load and holds slot (lane & 15) of the code
+// row, so the per-entry bookkeeping (the division by T, the code-row loads, the shuffle for
+// gamma_j(s)) is issued once for two entries.  The halves' C(:,j) updates go one after the other
+// (two signals of atom j's list can share other atoms).  Leaves warp w's partials in
+// Cw[w * Kp + .] (zeroed by the caller), Yw[w * n + .] and g2w[w]; the caller synchronises.
+template <int NQ, bool FULLN, int NW>
+__device__ __forceinline__ void prepare_half_range(
+    const float* __restrict__ X, int n, int T, int Kp, const int32_t* __restrict__ idx,
+    const float* __restrict__ coef, const int32_t* __restrict__ nnz,
+    const int32_t* __restrict__ list, int64_t q0, int64_t q1, float* Cw, float* Yw, float* g2w) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int hl = lane & 15, half = lane >> 4;
-  const int j = blockIdx.x;
-  for (int i = threadIdx.x; i < NW * Kp; i += blockDim.x) Cw[i] = 0.f;
-  __syncthreads();
-  const int64_t q0 = start[j], q1 = start[j + 1];
   float* cw = Cw + (size_t)w * Kp;
   float4 acc[NQ];
 #pragma unroll
@@ -393,8 +384,93 @@ prepare_half_kernel(const float* __restrict__ X, int n, int T, int Kp,
     }
   }
   if (lane == 0) g2w[w] = g2;
+}
+
+// One CTA per atom over its whole list (the half-warp layout of prepare_half_range).
+template <int NQ, bool FULLN>
+__global__ void __launch_bounds__(kPrepThreads)
+prepare_half_kernel(const float* __restrict__ X, int n, int T, int Kp,
+                    const int32_t* __restrict__ idx, const float* __restrict__ coef,
+                    const int32_t* __restrict__ nnz, const int32_t* __restrict__ list,
+                    const int64_t* __restrict__ start, float* __restrict__ Y,
+                    float* __restrict__ gn2, float* __restrict__ C) {
+  constexpr int NW = kPrepThreads / 32;
+  extern __shared__ float sm[];
+  float* Cw = sm;                        // NW x Kp
+  float* Yw = sm + (size_t)NW * Kp;      // NW x n
+  __shared__ float g2w[NW];
+  const int j = blockIdx.x;
+  for (int i = threadIdx.x; i < NW * Kp; i += blockDim.x) Cw[i] = 0.f;
+  __syncthreads();
+  prepare_half_range<NQ, FULLN, NW>(X, n, T, Kp, idx, coef, nnz, list, start[j], start[j + 1],
+                                    Cw, Yw, g2w);
   __syncthreads();
   prepare_sum_warps<NW>(Cw, Yw, g2w, n, Kp, j, Y, gn2, C);
+}
+
+// Windowed preparation for X larger than L2: CTA b takes the entries of atom j = b % Kp whose
+// signals lie in window w = b / Kp (bpw blocks of kSigPerBlock signals; the list's per-block
+// offsets come from the count/scan kernels), so the CTAs resident at one time gather from one
+// window of X, which stays in L2 while every atom of the window reads it.  Each CTA writes its
+// partials [Y(:,j) (n) | C(:,j) (Kp) | ||gamma_j||^2 (1)] to part; prepare_win_reduce sums the
+// windows in order (deterministic).
+template <int NQ, bool FULLN>
+__global__ void __launch_bounds__(kPrepWinThreads, 4)
+prepare_win_kernel(const float* __restrict__ X, int n, int T, int Kp,
+                   const int32_t* __restrict__ idx, const float* __restrict__ coef,
+                   const int32_t* __restrict__ nnz, const int32_t* __restrict__ list,
+                   const int64_t* __restrict__ start, const int32_t* __restrict__ block_hist,
+                   int64_t nblk, int64_t bpw, float* __restrict__ part) {
+  constexpr int NW = kPrepWinThreads / 32;
+  extern __shared__ float sm[];
+  float* Cw = sm;                        // NW x Kp
+  float* Yw = sm + (size_t)NW * Kp;      // NW x n
+  __shared__ float g2w[NW];
+  const int j = (int)(blockIdx.x % (unsigned)Kp);
+  const int64_t win = blockIdx.x / (unsigned)Kp;
+  const int64_t b0 = win * bpw, b1 = b0 + bpw;
+  const int64_t q0 = start[j] + block_hist[(int64_t)j * nblk + b0];
+  const int64_t q1 = b1 < nblk ? start[j] + block_hist[(int64_t)j * nblk + b1] : start[j + 1];
+  for (int i = threadIdx.x; i < NW * Kp; i += blockDim.x) Cw[i] = 0.f;
+  __syncthreads();
+  prepare_half_range<NQ, FULLN, NW>(X, n, T, Kp, idx, coef, nnz, list, q0, q1, Cw, Yw, g2w);
+  __syncthreads();
+  float* out = part + ((size_t)win * Kp + j) * (size_t)(n + Kp + 1);
+  for (int r = threadIdx.x; r < n; r += blockDim.x) {
+    float a = 0.f;
+#pragma unroll
+    for (int ww = 0; ww < NW; ++ww) a += Yw[(size_t)ww * n + r];
+    out[r] = a;
+  }
+  for (int i = threadIdx.x; i < Kp; i += blockDim.x) {
+    float a = 0.f;
+#pragma unroll
+    for (int ww = 0; ww < NW; ++ww) a += Cw[(size_t)ww * Kp + i];
+    out[n + i] = a;
+  }
+  if (threadIdx.x == 0) {
+    float a = 0.f;
+#pragma unroll
+    for (int ww = 0; ww < NW; ++ww) a += g2w[ww];
+    out[n + Kp] = a;
+  }
+}
+
+// Y, C and gn2 from the windows' partials, summed in window order.
+__global__ void prepare_win_reduce(const float* __restrict__ part, int64_t nwin, int n, int Kp,
+                                   float* __restrict__ Y, float* __restrict__ gn2,
+                                   float* __restrict__ C) {
+  const int64_t row = (int64_t)n + Kp + 1;
+  const int64_t total = (int64_t)Kp * row;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    float a = 0.f;
+    for (int64_t w = 0; w < nwin; ++w) a += part[w * total + t];
+    const int64_t j = t / row, r = t - j * row;
+    if (r < n) Y[j * n + r] = a;
+    else if (r < n + Kp) C[j * Kp + (r - n)] = a;
+    else gn2[j] = a;
+  }
 }
 
 __global__ void init_state_kernel(int64_t N, int Kp, int32_t* __restrict__ unused,
@@ -1136,6 +1212,15 @@ int sweep_grid_size() {
 
 int64_t update_block_count(int64_t N) { return (N + kSigPerBlock - 1) / kSigPerBlock; }
 
+// Windows of ~32 MB of signals once X exceeds 96 MB (L2 is 129 MB): a window's signals are read
+// from HBM once and gathered from L2 by the T atoms of each signal's support.
+int64_t prepare_window_signals(int64_t N, int n, int T) {
+  constexpr int64_t kWindowBytes = 32ll << 20, kMinX = 96ll << 20;
+  if (T > 16 || n % 4 != 0 || n > 256 || N * n * 4 <= kMinX) return 0;
+  const int64_t w = std::max<int64_t>(1, kWindowBytes / (4ll * n) / kSigPerBlock) * kSigPerBlock;
+  return w < N ? w : 0;
+}
+
 cudaError_t launch_update_prepare(const UpdateArgs& a, cudaStream_t st) {
   if (a.N <= 0) return cudaSuccess;
   if (a.Kp > 1024 || a.n > kMaxN) return cudaErrorInvalidValue;
@@ -1179,7 +1264,29 @@ cudaError_t launch_update_prepare(const UpdateArgs& a, cudaStream_t st) {
   // the half-warp kernel when its layout fits (rows of X 16-byte aligned, one slot per lane)
   const bool half = a.T <= 16 && a.n % 4 == 0 && a.n <= 256 &&
                     (reinterpret_cast<uintptr_t>(a.X) & 15) == 0;
-  if (half && a.n <= 64) e = launch_nq(std::integral_constant<int, 1>());
+  if (half && a.prep_part && a.prep_win > 0 && a.prep_win % kSigPerBlock == 0 &&
+      a.prep_win < a.N) {
+    const int64_t nwin = (a.N + a.prep_win - 1) / a.prep_win;
+    const int64_t bpw = a.prep_win / kSigPerBlock;
+    const size_t wsm = sizeof(float) * ((size_t)(kPrepWinThreads / 32) * (a.Kp + a.n));
+    auto launch_win = [&](auto kern) -> cudaError_t {
+      cudaError_t e2 = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)wsm);
+      if (e2 != cudaSuccess) return e2;
+      kern<<<(unsigned)(nwin * a.Kp), kPrepWinThreads, wsm, st>>>(
+          a.X, a.n, a.T, a.Kp, a.idx, a.coef, a.nnz, a.list, a.start, a.block_hist, nblk, bpw,
+          a.prep_part);
+      if ((e2 = cudaGetLastError()) != cudaSuccess) return e2;
+      prepare_win_reduce<<<1216, 256, 0, st>>>(a.prep_part, nwin, a.n, a.Kp, a.Y, a.gn2, a.C);
+      return cudaGetLastError();
+    };
+    if (a.n <= 64) e = a.n == 64 ? launch_win(prepare_win_kernel<1, true>)
+                                 : launch_win(prepare_win_kernel<1, false>);
+    else if (a.n <= 128) e = a.n == 128 ? launch_win(prepare_win_kernel<2, true>)
+                                        : launch_win(prepare_win_kernel<2, false>);
+    else e = a.n == 256 ? launch_win(prepare_win_kernel<4, true>)
+                        : launch_win(prepare_win_kernel<4, false>);
+  } else if (half && a.n <= 64) e = launch_nq(std::integral_constant<int, 1>());
   else if (half && a.n <= 128) e = launch_nq(std::integral_constant<int, 2>());
   else if (half) e = launch_nq(std::integral_constant<int, 4>());
   else if (npl <= 2) e = launch_npl(std::integral_constant<int, 2>());

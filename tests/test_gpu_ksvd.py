@@ -146,7 +146,9 @@ def code_from_oracle(oracle_mod, X, D, T):
 
 
 # the list preparation has a half-warp kernel (T <= 16, n % 4 == 0, n <= 256) and a full-warp one:
-# the first three and (200, ...) take the half-warp kernel, (50, ...) and (96, ..., 20) the other
+# the first three and (200, ...) take the half-warp kernel, (50, ...) and (96, ..., 20) the other;
+# (64, 128, 400000, 4) has X = 102 MB, above the 96 MiB from which the preparation runs in
+# windows of 131,072 signals (four here, the last one short) and sums the windows' partials
 @pytest.mark.parametrize("n,K,N,T,seed,unused_atom", [
     (64, 256, 8000, 8, 20, False),
     (256, 1024, 20000, 16, 21, False),
@@ -154,6 +156,7 @@ def code_from_oracle(oracle_mod, X, D, T):
     (200, 512, 6000, 10, 23, False),
     (50, 128, 4000, 6, 24, False),
     (96, 256, 5000, 20, 25, False),
+    (64, 128, 400000, 4, 26, False),
 ])
 def test_update_matches_oracle(oracle_mod, cuda, n, K, N, T, seed, unused_atom):
     import torch
