@@ -668,18 +668,33 @@ struct Sweep {
     const int n = A.n, Kp = A.Kp;
     const float g2 = A.gn2[jn];
     if (k1 > k0 || c == 0) {
-      for (int r = gt; r < n; r += gsize) {
-        float acc = 0.f;
+      // two rows per thread at once (n <= 2 gsize in the usual split), so their loads share one
+      // round trip
+      for (int r0 = gt; r0 < n; r0 += 2 * gsize) {
+        const int r1 = r0 + gsize;
+        const bool two = r1 < n;
+        float acc0 = 0.f, acc1 = 0.f;
 #pragma unroll 8
-        for (int k = k0; k < k1; ++k) acc = fmaf(-v_s[k], __ldcg(A.D + (int64_t)k * n + r), acc);
-        if (c == 0) acc += A.Y[(int64_t)jn * n + r] + g2 * __ldcg(A.D + (int64_t)jn * n + r);
-        atomicAdd(avec_slot + r, acc);
+        for (int k = k0; k < k1; ++k) {
+          const float vk = v_s[k];
+          acc0 = fmaf(-vk, __ldcg(A.D + (int64_t)k * n + r0), acc0);
+          if (two) acc1 = fmaf(-vk, __ldcg(A.D + (int64_t)k * n + r1), acc1);
+        }
+        if (c == 0) {
+          acc0 += A.Y[(int64_t)jn * n + r0] + g2 * __ldcg(A.D + (int64_t)jn * n + r0);
+          if (two) acc1 += A.Y[(int64_t)jn * n + r1] + g2 * __ldcg(A.D + (int64_t)jn * n + r1);
+        }
+        atomicAdd(avec_slot + r0, acc0);
+        if (two) atomicAdd(avec_slot + r1, acc1);
       }
     }
     const int k4n = Kp >> 2;                          // Kp is a multiple of 128
     const int gw = gt >> 5, gnw = gsize >> 5;
     for (int i = k0 + gw; i < k1; i += gnw) {
       if (i == jx) continue;                          // a(jn)'d_jx is formed after the barrier
+      // P(i, jn) and G(i, jn) are loaded with the row of G, in the same round trip
+      const float pij = __ldcg(A.P + (int64_t)jn * Kp + i);
+      const float gij = __ldcg(A.G + (int64_t)jn * Kp + i);
       const float4* gi = reinterpret_cast<const float4*>(A.G + (int64_t)i * Kp);
       const float4* vv = reinterpret_cast<const float4*>(v_s);
       float acc = 0.f;
@@ -693,9 +708,7 @@ struct Sweep {
         }
       }
       acc = warp_sum(acc);
-      if (lane == 0)
-        aD_slot[i] = __ldcg(A.P + (int64_t)jn * Kp + i) - acc +
-                     g2 * __ldcg(A.G + (int64_t)jn * Kp + i);
+      if (lane == 0) aD_slot[i] = pij - acc + g2 * gij;
     }
   }
 
@@ -1120,8 +1133,6 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
   const int K = A.K, n = A.n, tid = threadIdx.x;
   constexpr int HALF = Sweep<NPL, HW, FULLN>::HALF;
   const int32_t* perm = A.perm + (A.iter_ctr ? (int64_t)(*A.iter_ctr) * K : 0);
-  // fewer than ~50 list entries per atom and CTA on average (measured: 26 faster, 103 slower)
-  const bool light = A.N * A.T < 50LL * K * gridDim.x;
   // every CTA checks the whole permutation itself, so all of them leave together or none does
   int bad = 0;
   for (int k = tid; k < A.Kp; k += blockDim.x) S.pos[k] = K;   // (an order with repeats: no skips)
@@ -1176,16 +1187,15 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
       constexpr int QUART = HALF / 2;
       if (S.c == 0)
         for (int r = gt; r < n; r += HALF) A.D[(int64_t)j * n + r] = S.a_s[r] / anorm;
-      // With few signals per atom and CTA the helpers set the phase's length, and the prefetch
-      // goes with the shorter refresh task; with many, the coefficient warps do, and the
-      // prefetch (whose lines the next phase reads) stays after the partials.
+      // The prefetch goes with the shorter refresh task: the next atom's partials (dependent
+      // rounds of L2 loads and atomics) are the longer helper task (measured at cfg2: partials
+      // 6.1 us per atom, refresh 1.6 us, the coefficient warps 5.4 us before the prefetch moved).
       if (gt < QUART) {
         S.refresh_gp(j, 1.f / anorm, true, gt, QUART);
-        if (light && jn >= 0) S.prefetch_next(jn, (jj + 1) & 1, gt, QUART);
+        if (jn >= 0) S.prefetch_next(jn, (jj + 1) & 1, gt, QUART);
       } else if (jn >= 0) {
         S.next_partials(jn, j, av_next, ad_next, gt - QUART, QUART);
         S.zero_row(jn, gt - QUART, QUART);
-        if (!light) S.prefetch_next(jn, (jj + 1) & 1, gt - QUART, QUART);
       }
       S.update_coefs(j, q0, cnt, anorm, jj & 1, &next_batch, &use_cnt);
     }
