@@ -123,6 +123,13 @@ def stage_bytes(cfg, N, stage):
         #                     twice (a'D product and C refresh), write the new coefficient
         return N * T * (n * 4) + 2 * N * T * T * 8 + N * T * 4
     if stage == "lists":    # idx/nnz twice (count, fill), list write, X gathered per entry
+        if T <= 16 and n % 4 == 0 and n <= 256 and N * n * 4 > (96 << 20):
+            # windowed preparation: each ~32 MB window of X (and its codes) is read from HBM
+            # once and gathered from L2; the windows' partials are written and read once
+            w = max(1, (32 << 20) // (4 * n) // 256) * 256
+            nwin = -(-N // w)
+            return (2 * N * T * 4 + N * T * 4 + N * T * 4 + N * n * 4 + N * T * 8
+                    + 2 * nwin * Kp * (n + Kp + 1) * 4)
         return 2 * N * T * 4 + N * T * 4 + N * T * (n * 4 + T * 8)
     if stage == "error":    # X once, the code once, the error vector
         return N * n * 4 + N * T * 8 + N * 4
