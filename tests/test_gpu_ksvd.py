@@ -148,7 +148,9 @@ def code_from_oracle(oracle_mod, X, D, T):
 # the list preparation has a half-warp kernel (T <= 16, n % 4 == 0, n <= 256) and a full-warp one:
 # the first three and (200, ...) take the half-warp kernel, (50, ...) and (96, ..., 20) the other;
 # (64, 128, 400000, 4) has X = 102 MB, above the 96 MiB from which the preparation runs in
-# windows of 131,072 signals (four here, the last one short) and sums the windows' partials
+# windows of 131,072 signals (four here, the last one short) and sums the windows' partials;
+# (200, 256, 130000, 6) runs the windowed kernel with rows that do not fill the last 16-byte
+# group of lanes (n = 200: four windows of 41,728 signals, the last one short)
 @pytest.mark.parametrize("n,K,N,T,seed,unused_atom", [
     (64, 256, 8000, 8, 20, False),
     (256, 1024, 20000, 16, 21, False),
@@ -157,6 +159,7 @@ def code_from_oracle(oracle_mod, X, D, T):
     (50, 128, 4000, 6, 24, False),
     (96, 256, 5000, 20, 25, False),
     (64, 128, 400000, 4, 26, False),
+    (200, 256, 130000, 6, 27, False),
 ])
 def test_update_matches_oracle(oracle_mod, cuda, n, K, N, T, seed, unused_atom):
     import torch
@@ -190,6 +193,38 @@ def test_update_matches_oracle(oracle_mod, cuda, n, K, N, T, seed, unused_atom):
     if unused_atom:
         assert st["replaced"][5] == 1
         np.testing.assert_allclose(from_dev(Dd)[:, 5], Dr[:, 5], atol=1e-5)
+    h.close()
+
+
+def test_update_with_unaligned_signals(oracle_mod, cuda):
+    """X starting 4 bytes past a 16-byte boundary (a view of a larger buffer): the half-warp
+    preparation, sweep and error kernels need 16-byte aligned signals, so the library takes the
+    warp-per-entry kernels, with the same results."""
+    import torch
+    from ksvd_gb300 import Handle
+
+    n, K, N, T = 64, 256, 8000, 8
+    X, D = problem(n, K, N, T, 28)
+    idx, coef, nnz = code_from_oracle(oracle_mod, X, D, T)
+    perm = np.random.default_rng(28).permutation(K).astype(np.int32)
+    coef32 = coef.astype(np.float32)
+    Dr, cr, st = oracle_mod.update(X.astype(np.float64), D.astype(np.float64), idx,
+                                   coef32.astype(np.float64), nnz, perm)
+    flat = torch.zeros(N * n + 1, dtype=torch.float32, device=cuda)
+    Xd = flat[1:].view(N, n)
+    Xd.copy_(to_dev(X, cuda))
+    assert Xd.data_ptr() % 16 == 4
+    h = Handle(n, K, T)
+    Dd = to_dev(D, cuda)
+    cd = torch.from_numpy(coef32).to(cuda)
+    idd, nnd = torch.from_numpy(idx).to(cuda), torch.from_numpy(nnz).to(cuda)
+    h.update_dictionary(Dd, Xd, idd, cd, nnd, perm)
+    r, e = h.error(Dd, Xd, idd, cd, nnd, want_err=True)
+    h.synchronize()
+    assert rel_rmse(from_dev(Dd), Dr) <= REL_TOL
+    assert rel_rmse(cd.cpu().numpy(), cr) <= REL_TOL
+    rr, er = oracle_mod.error(X.astype(np.float64), Dr, idx, cr, nnz, st["bitmap"])
+    assert abs(r - rr) / rr <= REL_TOL
     h.close()
 
 
