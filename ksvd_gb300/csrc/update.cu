@@ -1190,8 +1190,9 @@ __global__ void __launch_bounds__(kSweepThreads, 1) sweep_kernel(SweepArgs A) {
       if (S.c == 0)
         for (int r = gt; r < n; r += HALF) A.D[(int64_t)j * n + r] = S.a_s[r] / anorm;
       // The prefetch goes with the shorter refresh task: the next atom's partials (dependent
-      // rounds of L2 loads and atomics) are the longer helper task (measured at cfg2: partials
-      // 6.1 us per atom, refresh 1.6 us, the coefficient warps 5.4 us before the prefetch moved).
+      // rounds of L2 loads and atomics) are the longer helper task (measured at n=256, K=1024,
+      // N=1M, T=16: partials 6.1 us per atom, refresh 1.6 us, the coefficient warps 5.4 us
+      // before the prefetch moved).
       if (gt < QUART) {
         S.refresh_gp(j, 1.f / anorm, true, gt, QUART);
         if (jn >= 0) S.prefetch_next(jn, (jj + 1) & 1, gt, QUART);
