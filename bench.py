@@ -37,9 +37,15 @@ if ROOT not in sys.path:
 # library kernels per ksvd_iterate call: copy_pad_cols, normcols, Gram (mixed: + BF16 splits of D
 # and X); per iteration: D'X, OMP, Gram, 4 list kernels, init_state, prepare, P = D'Y, sweep,
 # error + rmse, Gram, coherence + clear_seq, advance_counter (mixed: + 3 BF16 splits of D and
-# the FP16 copy of G for Batch-OMP)
+# the FP16 copy of G and its column coherences for Batch-OMP); the windowed preparation (X above
+# 96 MiB, T <= 16, n % 4 == 0, n <= 256) adds the reduction of the windows' partials
 KERNELS_PER_CALL = {"fp32": 3, "mixed": 5}
-KERNELS_PER_ITER = {"fp32": 17, "mixed": 21}
+KERNELS_PER_ITER = {"fp32": 17, "mixed": 22}
+
+
+def windowed_prep(n, T, N):
+    """Whether the list preparation runs in windows of X (the library's rule)."""
+    return T <= 16 and n % 4 == 0 and n <= 256 and N * n * 4 > (96 << 20)
 
 
 def peaks():
@@ -123,7 +129,7 @@ def stage_bytes(cfg, N, stage):
         #                     twice (a'D product and C refresh), write the new coefficient
         return N * T * (n * 4) + 2 * N * T * T * 8 + N * T * 4
     if stage == "lists":    # idx/nnz twice (count, fill), list write, X gathered per entry
-        if T <= 16 and n % 4 == 0 and n <= 256 and N * n * 4 > (96 << 20):
+        if windowed_prep(n, T, N):
             # windowed preparation: each ~32 MB window of X (and its codes) is read from HBM
             # once and gathered from L2; the windows' partials are written and read once
             w = max(1, (32 << 20) // (4 * n) // 256) * 256
@@ -806,7 +812,7 @@ def main():
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": KERNELS_PER_CALL[args.precision] +
-            args.steps * KERNELS_PER_ITER[args.precision],
+            args.steps * (KERNELS_PER_ITER[args.precision] + windowed_prep(cfg.n, cfg.T, N)),
             "clocks": clocks,
             "rmse_last": rms[-1] if rms else None,
             "error_vs_fp64_oracle": fp64_check,
