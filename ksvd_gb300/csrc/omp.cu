@@ -536,15 +536,26 @@ omp_kernel(const float* __restrict__ G, const uint16_t* __restrict__ Gh,
   bool numeric_bad = false;
   const bool emode = eps2 != nullptr;
   if constexpr (QUEUE) {
-    // resident grid: warps claim kOmpClaim signals at a time from *queue (zeroed before the
-    // launch); early stops make signals uneven, and the last claims even the SMs out
+    // resident grid: warps claim kOmpClaim signals at a time from *queue (a signal counter,
+    // zeroed before the launch); early stops make signals uneven, and once fewer than
+    // kOmpClaim signals per resident warp remain the claims shrink to one signal, so the last
+    // warps finish close together (the size is chosen from a plain read of the counter; the
+    // claimed ranges stay disjoint and cover [0, N) whatever the size)
+    const unsigned long long tail =
+        (unsigned long long)gridDim.x * kOmpWarps * kOmpClaim;
     for (;;) {
       unsigned long long cl = 0;
-      if (lane == 0) cl = atomicAdd(queue, 1ull);
+      int sz = kOmpClaim;
+      if (lane == 0) {
+        const unsigned long long seen = *((volatile unsigned long long*)queue);
+        if (seen + tail >= (unsigned long long)N) sz = 1;
+        cl = atomicAdd(queue, (unsigned long long)sz);
+      }
       cl = __shfl_sync(KSVD_FULL_MASK, cl, 0);
-      const int64_t s0 = (int64_t)cl * kOmpClaim;
+      sz = __shfl_sync(KSVD_FULL_MASK, sz, 0);
+      const int64_t s0 = (int64_t)cl;
       if (s0 >= N) break;
-      const int64_t s1 = min(N, s0 + kOmpClaim);
+      const int64_t s1 = min(N, s0 + sz);
       for (int64_t s = s0; s < s1; ++s)
         omp_signal<KPL, TMAX, H16>(G, Gh, mu_col, ldg, A0 + s * lda, K, T, emode,
                                    emode ? eps2[s] : 0.f, emode ? xnorm2[s] : 0.f,

