@@ -166,13 +166,13 @@ KERNEL_SOURCES = {"omp": ("omp.cu",)}
 # (n, K, T, precision, fingerprint) -> (bytes per signal, L2 %, issue %): omp_kernel<32, 32, H16, 1>
 # at 100,000 signals, dram__bytes_read.sum + dram__bytes_write.sum per signal
 MEASURED_OMP = {
-    (256, 1024, 16, "mixed", "131851db534dfae7"): ((415998976 + 7024896) / 100_000, 44.93, 67.97),
-    (256, 1024, 16, "fp32", "131851db534dfae7"): ((413822464 + 7335168) / 100_000, 75.32, 52.30),
+    (256, 1024, 16, "mixed", "9ea78b3f92b4e8e6"): ((415949056 + 7203328) / 100_000, 46.35, 69.25),
+    (256, 1024, 16, "fp32", "9ea78b3f92b4e8e6"): ((414021120 + 7380224) / 100_000, 77.33, 52.93),
 }
 # omp_batched_kernel<64> on the cfg3 mix scaled to 293,494 signals (same source fingerprint):
 # DRAM bytes per signal -- far above the algorithmic bytes, the support columns of 64 Gram
 # matrices miss L2 (86 % hit rate)
-MEASURED_BATCHED = {"131851db534dfae7": (43017219072 + 95583744) / 293494}
+MEASURED_BATCHED = {"9ea78b3f92b4e8e6": (42793800192 + 95375360) / 293494}
 
 
 def source_fingerprint(stage):
