@@ -43,8 +43,7 @@ def test_rmse_noalloc_matches_ksvd_error(cuda):
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     N = X.shape[0]
     # set-up call: the first call on a device may make the CUDA driver load the library's device
-    # code
-    # (the static scratch array becomes resident then); nothing is allocated after it
+    # code (the static scratch array becomes resident then); nothing is allocated after it
     st, _ = _call(lib, c, D, X, N, idx, coef, nnz, stream)
     assert st == 0, lib.ksvd_last_error(None).decode()
     torch.cuda.synchronize()
