@@ -165,7 +165,12 @@ KSVD_API ksvd_status ksvd_omp(ksvd_handle* handle, const float* D, const float* 
  * atom indices, or NULL to draw one from the handle's seed).  Updates D and coef in place;
  * idx/nnz are unchanged.  Also resets the unused-signal bookkeeping first, as
  * ExecuteIterations does with its init kernel.  Replaces initialize() + updateDictionary(perm)
- * (KSVD.cu:97-114, DictionaryUpdate.cu:45-203). */
+ * (KSVD.cu:97-114, DictionaryUpdate.cu:45-203).
+ * Speed (not results): with T <= 16, n % 4 == 0, n <= 256 and X 16-byte aligned the sweep and
+ * its list preparation use their half-warp kernels (and, once X exceeds 96 MiB, the windowed
+ * preparation, which needs about ceil(N / W) * Kp * (n + Kp + 1) floats of workspace, W the
+ * signals in 32 MB); other inputs take the warp-per-entry kernels.  The same holds for
+ * ksvd_error (with D 16-byte aligned too) and for the stages inside ksvd_iterate. */
 KSVD_API ksvd_status ksvd_update_dictionary(ksvd_handle* handle, float* D, const float* X, int64_t N,
                                    const int32_t* idx, float* coef, const int32_t* nnz,
                                    const int32_t* perm);
