@@ -359,15 +359,28 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
           b[j] = q < i ? __ldg(G + (int64_t)ind[j] * ldg + p) : 0.f;
           w[j] = 0.f;
         }
-        for (int r = 0; r < i; ++r) {
-          const int rl = r & 31, rj = r >> 5;
-          const float wr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(b, rj), rl) * L[lidx<TMAX>(r, r)];
+        // two rows per loop step, with the one-row sweep's operations in its order (row r + 1
+        // takes row r's term before its own division), so the results are the same bits
+        int r = 0;
+        for (; r + 1 < i; r += 2) {
+          const int rl = r & 31, rj = r >> 5, rl1 = (r + 1) & 31, rj1 = (r + 1) >> 5;
+          const float br = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(b, rj), rl);
+          const float br1 = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(b, rj1), rl1);
+          const float wr = br * L[lidx<TMAX>(r, r)];
+          const float wr1 = fmaf(-L[lidx<TMAX>(r + 1, r)], wr, br1) * L[lidx<TMAX>(r + 1, r + 1)];
           if (lane == rl) put<SPL>(w, rj, wr);
+          if (lane == rl1) put<SPL>(w, rj1, wr1);
 #pragma unroll
           for (int j = 0; j < SPL; ++j) {
             const int q = lane + 32 * j;
-            if (q > r && q < i) b[j] = fmaf(-L[lidx<TMAX>(q, r)], wr, b[j]);
+            if (q > r + 1 && q < i)
+              b[j] = fmaf(-L[lidx<TMAX>(q, r + 1)], wr1, fmaf(-L[lidx<TMAX>(q, r)], wr, b[j]));
           }
+        }
+        if (r < i) {                         // the last row when i is odd
+          const int rl = r & 31, rj = r >> 5;
+          const float wr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(b, rj), rl) * L[lidx<TMAX>(r, r)];
+          if (lane == rl) put<SPL>(w, rj, wr);
         }
         float ss = 0.f, wy = 0.f;
 #pragma unroll
@@ -407,15 +420,26 @@ __device__ __forceinline__ void omp_signal(const float* __restrict__ G,
         float t[SPL];
 #pragma unroll
         for (int j = 0; j < SPL; ++j) t[j] = y[j];
-        for (int r = i - 1; r >= 0; --r) {
-          const int rl = r & 31, rj = r >> 5;
-          const float cr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(t, rj), rl) * L[lidx<TMAX>(r, r)];
+        // two rows per loop step, in the one-row sweep's order of operations (same bits)
+        int r = i - 1;
+        for (; r >= 1; r -= 2) {
+          const int rl = r & 31, rj = r >> 5, rl1 = (r - 1) & 31, rj1 = (r - 1) >> 5;
+          const float tr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(t, rj), rl);
+          const float tr1 = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(t, rj1), rl1);
+          const float cr = tr * L[lidx<TMAX>(r, r)];
+          const float cr1 = fmaf(-L[lidx<TMAX>(r, r - 1)], cr, tr1) * L[lidx<TMAX>(r - 1, r - 1)];
           if (lane == rl) put<SPL>(c, rj, cr);
+          if (lane == rl1) put<SPL>(c, rj1, cr1);
 #pragma unroll
           for (int j = 0; j < SPL; ++j) {
             const int q = lane + 32 * j;
-            if (q < r) t[j] = fmaf(-L[lidx<TMAX>(r, q)], cr, t[j]);
+            if (q < r - 1)
+              t[j] = fmaf(-L[lidx<TMAX>(r - 1, q)], cr1, fmaf(-L[lidx<TMAX>(r, q)], cr, t[j]));
           }
+        }
+        if (r == 0) {                        // row 0 when i is odd
+          const float cr = __shfl_sync(KSVD_FULL_MASK, pick<SPL>(t, 0), 0) * L[lidx<TMAX>(0, 0)];
+          if (lane == 0) put<SPL>(c, 0, cr);
         }
       }
       // ---- alpha = alpha0 - G(:, I) c   (not needed after the last atom)
