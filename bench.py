@@ -166,13 +166,13 @@ KERNEL_SOURCES = {"omp": ("omp.cu",)}
 # (n, K, T, precision, fingerprint) -> (bytes per signal, L2 %, issue %): omp_kernel<32, 32, H16, 1>
 # at 100,000 signals, dram__bytes_read.sum + dram__bytes_write.sum per signal
 MEASURED_OMP = {
-    (256, 1024, 16, "mixed", "9ea78b3f92b4e8e6"): ((415949056 + 7203328) / 100_000, 46.35, 69.25),
-    (256, 1024, 16, "fp32", "9ea78b3f92b4e8e6"): ((414021120 + 7380224) / 100_000, 77.33, 52.93),
+    (256, 1024, 16, "mixed", "278aec7dbdb97848"): ((416187904 + 7526656) / 100_000, 46.98, 71.26),
+    (256, 1024, 16, "fp32", "278aec7dbdb97848"): ((413833216 + 7440128) / 100_000, 77.82, 53.98),
 }
 # omp_batched_kernel<64> on the cfg3 mix scaled to 293,494 signals (same source fingerprint):
 # DRAM bytes per signal -- far above the algorithmic bytes, the support columns of 64 Gram
 # matrices miss L2 (86 % hit rate)
-MEASURED_BATCHED = {"9ea78b3f92b4e8e6": (42793800192 + 95375360) / 293494}
+MEASURED_BATCHED = {"278aec7dbdb97848": (42805705216 + 95426816) / 293494}
 
 
 def source_fingerprint(stage):
